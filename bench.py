@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Benchmark of Muscle.jl's binary_einsum on one GB300: ComplexF64 contraction
+in the emulated (Ozaki, tcgen05) form versus native FP64 (DMMA).
+
+Workload (precision form): A(i,k1,k2) = 8192x128x64, B(k2,j,k1) = 64x8192x128,
+ComplexF64 with log-uniform magnitudes over 2^-20..2^20 and uniform phase
+(PCG64 seed 0); the contraction over k1, k2 gives C(i,j) with M = N = K = 8192,
+8 M N K = 4.40e12 algorithmic flops. Operands are 1 GiB each, larger than L2,
+so no flush is needed between steps.
+
+One JSON line on rank 0:
+  value        algorithmic TFLOP/s of the Ozaki form (device-resident inputs)
+  e2e          same metric through the public API with host buffers, the
+               host->device copies of A, B and the device->host copy of C
+               inside the timed region
+  native       the plain form (FP64 DMMA) on the same shapes
+  rel_err      ||C_ozaki - C_fp64|| / ||C_fp64|| (Frobenius), C_fp64 = plain form
+  roofline     the Ozaki GEMM kernel: tensor-pipe flops per launch / its
+               CUDA-event duration, against the measured dense bf16 peak
+  cpu_baseline the CPU oracle (permute -> OpenBLAS zgemm -> permute) on a
+               bounded row sample of the same workload, all host threads
+
+--impl reference times that CPU path alone (the reference's own host path
+restated; Muscle.jl itself is Julia, which this machine does not have).
+Multi-GPU: each rank runs an independent replica of the workload (the
+contraction is not sharded), value = total flops of all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "muscle.jl_gb300", "python"), ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "C64 einsum TFLOP/s, emulated vs native FP64 @1e-13 rel err; served p50/p99 ms"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--slices", type=int, default=7)
+    ap.add_argument("--n", type=int, default=8192, help="M = N of the precision workload")
+    ap.add_argument("--native-steps", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
+    return ap.parse_args()
+
+
+def workload_config(n):
+    return {"workload": "precision form: ComplexF64 A(i,k1,k2) x B(k2,j,k1) -> C(i,j)",
+            "A": [n, 128, 64], "B": [64, n, 128], "M": n, "N": n, "K": 128 * 64,
+            "inputs": "log-uniform |z| in 2^-20..2^20, uniform phase, PCG64 seed 0",
+            "l2": "operands 1 GiB each > 129 MB L2; no flush"}
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["bf16_tflops"], p["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the Ozaki GEMM from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ozaki_gemm_c64_8192.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_full_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_sample(n, slices_target_s, seed=0):
+    """Times the CPU oracle on the first rows of A (same columns of B)."""
+    import oracle.muscle_ref as ref
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+
+    def run(rows):
+        a = np.asfortranarray(ref.loguniform_complex(rng, (rows, 128, 64)))
+        b = np.asfortranarray(ref.loguniform_complex(rng, (64, n, 128)))
+        t0 = time.perf_counter()
+        ref.contract(a, ["i", "k1", "k2"], b, ["k2", "j", "k1"], ["i", "j"])
+        dt = time.perf_counter() - t0
+        return 8.0 * rows * n * 8192 / dt, dt
+
+    rate, _ = run(64)  # calibration (includes B's permutation)
+    rows = int(max(64, min(n, rate * slices_target_s / (8.0 * n * 8192))))
+    rate, dt = run(rows)
+    return {"value": rate / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"rows i=1..{rows} of A (of {n}), full B; {dt:.1f} s; permute -> OpenBLAS zgemm -> permute"}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if os.environ.get("MGB_BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+    return ws, rank, local
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    cb = cpu_sample(args.n, args.cpu_seconds)
+    steps = []
+    for _ in range(max(1, args.steps)):
+        steps.append(cpu_sample(args.n, args.cpu_seconds / 2)["value"])
+    val = statistics.median(steps)
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": workload_config(args.n),
+            "cpu_baseline": {**cb, "value": val},
+            "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of Muscle.jl's BackendBase (Julia is not installed on this machine)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    import torch
+
+    import muscle_gb300 as m
+    from muscle_gb300 import _lib
+    import oracle.muscle_ref as ref
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.n
+    (a, ia), (b, ib), ic = ref.gen_config3(seed=0, n=n)
+    a_h = torch.from_numpy(a).pin_memory()
+    b_h = torch.from_numpy(b).pin_memory()
+    A = a_h.to(dev)  # column-major strides preserved
+    B = b_h.to(dev)
+    C = m.empty_colmajor([n, n], torch.complex128, dev)
+    Cn = m.empty_colmajor([n, n], torch.complex128, dev)
+    c_h = torch.empty_like(C, device="cpu").pin_memory()
+    plan = m.contraction_plan(A, [m.Index(x) for x in ia], B, [m.Index(x) for x in ib], C,
+                              [m.Index(x) for x in ic], "ozaki", args.slices)
+    pln = m.contraction_plan(A, [m.Index(x) for x in ia], B, [m.Index(x) for x in ib], Cn,
+                             [m.Index(x) for x in ic], "plain", 0)
+    ws_t = torch.empty(max(plan.workspace_bytes, 1), dtype=torch.uint8, device=dev)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+
+    def step(p=plan, out=C):
+        _lib.check(lib.mgb_contract(p.handle, A.data_ptr(), B.data_ptr(), out.data_ptr(), ws_t.data_ptr(),
+                                    ws_t.numel(), stream.cuda_stream), lib)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1), ws)
+    barrier(ws)
+    flops = plan.flops
+    value = flops * ws * args.steps / (ms / 1e3) / 1e12
+    launches_per_step = 5  # 2 exponent scans, 2 slicers, 1 tcgen05 GEMM (plus 2 memsets)
+
+    # kernel timing for the roofline: phase events around the GEMM launch
+    lib.mgb_plan_set_timing(plan.handle, 1)
+    pre, mainv = [], []
+    import ctypes
+
+    for _ in range(args.steps):
+        step()
+        fp, fm = ctypes.c_float(), ctypes.c_float()
+        _lib.check(lib.mgb_plan_timing(plan.handle, ctypes.byref(fp), ctypes.byref(fm)), lib)
+        pre.append(fp.value)
+        mainv.append(fm.value)
+    lib.mgb_plan_set_timing(plan.handle, 0)
+    gemm_ms = statistics.mean(mainv)
+    S = args.slices
+    pairs = S * (S + 1) // 2
+    tensor_flops = 2.0 * pairs * n * (2 * n) * (2 * 8192)
+    bf16_peak, hbm_peak, peak_kind = peaks()
+    achieved = tensor_flops / (gemm_ms / 1e3) / 1e12
+    traffic = ncu_traffic()
+
+    # native FP64 (DMMA) on the same shapes: the FP64 reference for the error
+    torch.cuda.synchronize()
+    en0, en1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    step(pln, Cn)  # warm-up
+    torch.cuda.synchronize()
+    en0.record(stream)
+    for _ in range(args.native_steps):
+        step(pln, Cn)
+    en1.record(stream)
+    torch.cuda.synchronize()
+    native_ms = en0.elapsed_time(en1) / args.native_steps
+    native = flops / (native_ms / 1e3) / 1e12
+    step()
+    torch.cuda.synchronize()
+    rel_err = (torch.linalg.vector_norm((C - Cn).flatten()) / torch.linalg.vector_norm(Cn.flatten())).item()
+
+    # end to end through the public API with host buffers
+    def e2e_step():
+        A.copy_(a_h, non_blocking=True)
+        B.copy_(b_h, non_blocking=True)
+        step()
+        c_h.copy_(C, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ee0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    ee1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(ee0.elapsed_time(ee1), ws)
+    e2e = flops * ws * args.steps / (e2e_ms / 1e3) / 1e12
+    status = m.device_status(dev)
+
+    cpu = None
+    if rank == 0 and ws == 1:
+        cpu = cpu_sample(n, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic", "config": workload_config(n),
+            "form": f"ozaki S={S} (bf16 digits of 7 bits on tcgen05.mma kind::f16, exact int accumulation)",
+            "rel_err": rel_err, "rel_err_reference": "plain FP64 DMMA result on the same inputs",
+            "native": {"value": native, "unit": "TFLOP/s", "ms_per_step": native_ms, "form": "plain FP64 DMMA (4M)"},
+            "speedup_vs_native": value / native,
+            "e2e": {"value": e2e, "unit": "TFLOP/s", "ms_per_step": e2e_ms / args.steps,
+                    "h2d_bytes_per_step": A.numel() * 16 + B.numel() * 16, "d2h_bytes_per_step": C.numel() * 16},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": achieved / bf16_peak, "traffic": traffic, "peak_kind": f"bf16 dense burst ({peak_kind})",
+                         "kernel": "k_oz_gemm", "kernel_ms": gemm_ms, "prepass_ms": statistics.mean(pre),
+                         "work": f"2 x {pairs} slice pairs x M x 2N x 2K bf16 flops per launch"},
+            "gpu_launches": launches_per_step * args.steps,
+            "device_status": status,
+            "clocks": clk.summary(),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

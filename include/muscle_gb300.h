@@ -1,0 +1,156 @@
+/*
+ * muscle_gb300.h — C ABI of libmuscle_gb300.so, a GB300 (sm_103a) backend for
+ * Muscle.jl's tensor contractions.
+ *
+ * The library replaces the device branch of Muscle.jl's operation front-ends:
+ *   binary_einsum(::Backend, inds_c, a, b)  src/Operations/binary_einsum.jl:50
+ *   binary_einsum!(::Backend, c, a, b)      src/Operations/binary_einsum.jl:68
+ *   unary_einsum(::Backend, inds_y, x)      src/Operations/unary_einsum.jl:35
+ *   unary_einsum!(::Backend, y, x)          src/Operations/unary_einsum.jl:44
+ * whose CUDA implementation is cuTENSOR.contract! in ext/MuscleCUDAExt.jl:10-41
+ * (label -> integer mode mapping at :24-27, alpha = 1, beta = 0 at :29-38).
+ *
+ * Conventions
+ *  - A tensor is described by its element type, rank, integer mode labels,
+ *    extents and strides in ELEMENTS (Julia's `strides`, column-major when the
+ *    array is dense). strides == NULL means dense column-major.
+ *  - Device buffers are owned by the caller; the library never frees them.
+ *  - Every entry returns an mgb_status; MGB_OK == 0. A per-thread message is
+ *    available from mgb_last_error().
+ *  - Streams are passed as `void*` (a cudaStream_t; NULL = legacy default).
+ *  - Plans are immutable after creation and may be executed concurrently on
+ *    different streams with different workspaces.
+ */
+#ifndef MUSCLE_GB300_H
+#define MUSCLE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGB_MAX_RANK 16
+
+typedef enum mgb_status {
+    MGB_OK = 0,
+    MGB_ERR_ARGUMENT = 1,           /* Julia ArgumentError (binary_einsum.jl:54,82-83) */
+    MGB_ERR_DIMENSION_MISMATCH = 2, /* Julia DimensionMismatch (Tensor.jl:23)          */
+    MGB_ERR_UNSUPPORTED = 3,        /* combination not implemented by the chosen form  */
+    MGB_ERR_WORKSPACE = 4,          /* workspace missing or too small                  */
+    MGB_ERR_CUDA = 5,               /* CUDA runtime error (message has details)        */
+    MGB_ERR_DEVICE_TIMEOUT = 6,     /* a bounded device-side wait gave up              */
+    MGB_ERR_OUT_OF_MEMORY = 7,      /* byte budget exceeded (serving admission)        */
+    MGB_ERR_NOT_FINITE = 8          /* non-finite input met by an emulated form        */
+} mgb_status;
+
+typedef enum mgb_dtype {
+    MGB_F32 = 0, /* Float32     */
+    MGB_F64 = 1, /* Float64     */
+    MGB_C32 = 2, /* ComplexF32  */
+    MGB_C64 = 3  /* ComplexF64  */
+} mgb_dtype;
+
+typedef enum mgb_form {
+    MGB_FORM_AUTO = 0,   /* OZAKI for F64/C64 results, BF16X3 for F32/C32        */
+    MGB_FORM_PLAIN = 1,  /* native arithmetic: FP64 DMMA / FP32 FFMA              */
+    MGB_FORM_OZAKI = 2,  /* FP64/C64 as exact bf16 integer slices on tcgen05      */
+    MGB_FORM_BF16X3 = 3  /* FP32/C32 as 3-piece bf16 split products on tcgen05    */
+} mgb_form;
+
+typedef struct mgb_tensor_desc {
+    int32_t dtype;            /* mgb_dtype                                    */
+    int32_t rank;             /* 0 .. MGB_MAX_RANK                            */
+    const int32_t *modes;     /* rank integer labels                          */
+    const int64_t *extents;   /* rank extents (>= 0)                          */
+    const int64_t *strides;   /* rank strides in elements, or NULL (dense)    */
+} mgb_tensor_desc;
+
+typedef struct mgb_plan_s *mgb_plan;
+
+/* Summary of a plan, for callers that report work or pick workspaces. */
+typedef struct mgb_plan_info {
+    int64_t m, n, k, batch;   /* folded GEMM view: left, right, contracted, hyper */
+    int32_t form;             /* resolved mgb_form                               */
+    int32_t slices;           /* Ozaki slice count (0 when not emulated)         */
+    int32_t compute_dtype;    /* promoted element type of the result             */
+    int32_t permute_a, permute_b, permute_c; /* 1 when PLAIN stages a permute     */
+    double flops;             /* algorithmic: 8MNK complex, 2MNK real (x batch)  */
+    uint64_t workspace_bytes; /* bytes mgb_contract needs                        */
+} mgb_plan_info;
+
+/* ---- binary contraction: C[modes_c] = sum A[modes_a] * B[modes_b] ---------
+ * Mode classes follow cuTENSOR semantics used by ext/MuscleCUDAExt.jl:36-38:
+ * a mode in A and B but not C is contracted; a mode in A, B and C is a batch
+ * (hyper) mode; a mode in exactly one operand and C is free. Any other pattern
+ * is MGB_ERR_ARGUMENT. The result element type is promote_eltype(A, B)
+ * (ext/MuscleCUDAExt.jl:16) and C must have it. alpha = 1, beta = 0.
+ * slices: Ozaki slice count (0 = default 7); ignored by other forms.       */
+int mgb_contraction_plan(mgb_plan *plan, const mgb_tensor_desc *a,
+                         const mgb_tensor_desc *b, const mgb_tensor_desc *c,
+                         int32_t form, int32_t slices);
+int mgb_contract(mgb_plan plan, const void *A, const void *B, void *C,
+                 void *workspace, uint64_t workspace_bytes, void *stream);
+
+/* ---- unary contraction: Y[modes_y] = sum over the other modes of X --------
+ * Repeated labels in X select a diagonal (test/integration/omeinsum.jl:6-100,
+ * ext/MuscleOMEinsumExt.jl:25-38). modes_y must be distinct and a subset of
+ * modes_x (ext/MuscleOMEinsumExt.jl:32). X and Y share the element type.   */
+int mgb_unary_plan(mgb_plan *plan, const mgb_tensor_desc *x,
+                   const mgb_tensor_desc *y);
+int mgb_unary(mgb_plan plan, const void *X, void *Y, void *workspace,
+              uint64_t workspace_bytes, void *stream);
+
+/* ---- permutation: Y[modes_y] = X[modes_x], modes_y a permutation of modes_x
+ * (Base.permutedims via src/Tensor.jl:316-319). Element types may differ only
+ * by real -> complex promotion of the same precision or F32 -> F64.        */
+int mgb_permute(const mgb_tensor_desc *x, const mgb_tensor_desc *y,
+                const void *X, void *Y, void *stream);
+
+int mgb_plan_info_get(mgb_plan plan, mgb_plan_info *info);
+/* Phase timing for benchmarks. When enabled, mgb_contract records CUDA events
+ * on its launch stream before its pre-pass kernels (scales, slices or
+ * operand conversion), before its main contraction kernel and after it;
+ * mgb_plan_timing synchronises on the last call's events and returns the two
+ * elapsed times in milliseconds. The events belong to the plan: while timing
+ * is enabled, execute the plan from one thread and one stream at a time. */
+int mgb_plan_set_timing(mgb_plan plan, int32_t enable);
+int mgb_plan_timing(mgb_plan plan, float *prepass_ms, float *main_ms);
+int mgb_plan_workspace_size(mgb_plan plan, uint64_t *bytes);
+int mgb_plan_destroy(mgb_plan plan);
+
+/* ---- grouped (batched) contractions ---------------------------------------
+ * Many independent plans executed by one persistent grouped launch per arith-
+ * metic class. Operand pointers are device pointers. The group is immutable;
+ * the pointer arrays are copied at creation (mgb_group_update may replace
+ * them before a later execute, e.g. for a CUDA-graph replay with new data).
+ * The ensemble of a PEPS sweep is the motivating case
+ * (ext/MuscleDaggerExt/binary_einsum.jl:64-119 runs such independent pairs
+ * as separate tasks).                                                      */
+typedef struct mgb_group_s *mgb_group;
+int mgb_group_create(mgb_group *group, const mgb_plan *plans, int32_t count,
+                     const void *const *A, const void *const *B,
+                     void *const *C);
+int mgb_group_update(mgb_group group, const void *const *A,
+                     const void *const *B, void *const *C);
+int mgb_group_workspace_size(mgb_group group, uint64_t *bytes);
+int mgb_group_execute(mgb_group group, void *workspace,
+                      uint64_t workspace_bytes, void *stream);
+/* Tile schedule of the grouped kernel: tile index per shape class. The
+ * autotuner (host side) writes it; -1 = built-in heuristic.               */
+int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan);
+int mgb_group_destroy(mgb_group group);
+
+/* ---- status ---------------------------------------------------------------*/
+const char *mgb_last_error(void);
+/* Reads and clears the device-side status word written by bounded waits and
+ * non-finite checks of kernels launched on `stream` (synchronises it).     */
+int mgb_device_status(void *stream, int32_t *status);
+/* Library version string. */
+const char *mgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MUSCLE_GB300_H */

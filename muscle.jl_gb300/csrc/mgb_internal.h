@@ -1,0 +1,139 @@
+// Internal declarations shared by the libmuscle_gb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "muscle_gb300.h"
+
+namespace mgb {
+
+constexpr int kMaxRank = MGB_MAX_RANK;
+
+// Per-thread error message behind mgb_last_error().
+void set_error(const std::string &msg);
+int fail(int status, const std::string &msg);
+int cuda_fail(cudaError_t err, const char *what);
+
+#define MGB_CUDA_CHECK(expr)                                  \
+    do {                                                      \
+        cudaError_t _e = (expr);                              \
+        if (_e != cudaSuccess) return ::mgb::cuda_fail(_e, #expr); \
+    } while (0)
+
+inline int elem_bytes(int dtype) {
+    switch (dtype) {
+    case MGB_F32: return 4;
+    case MGB_F64: return 8;
+    case MGB_C32: return 8;
+    case MGB_C64: return 16;
+    }
+    return 0;
+}
+inline bool is_complex(int dtype) { return dtype == MGB_C32 || dtype == MGB_C64; }
+inline bool is_double(int dtype) { return dtype == MGB_F64 || dtype == MGB_C64; }
+inline bool valid_dtype(int dtype) { return dtype >= MGB_F32 && dtype <= MGB_C64; }
+// Base.promote_eltype over {Float32, Float64, ComplexF32, ComplexF64}.
+inline int promote(int a, int b) {
+    bool c = is_complex(a) || is_complex(b);
+    bool d = is_double(a) || is_double(b);
+    return c ? (d ? MGB_C64 : MGB_C32) : (d ? MGB_F64 : MGB_F32);
+}
+
+// A folded group of modes and the strides it has in up to three tensors.
+// Linear index i in [0, size) decomposes mixed-radix with mode 0 fastest.
+struct ModeGroup {
+    int32_t n = 0;
+    int64_t ext[kMaxRank];
+    int64_t str[3][kMaxRank];  // stride in tensor 0/1/2 (elements), 0 when absent
+    int64_t size() const {
+        int64_t s = 1;
+        for (int i = 0; i < n; ++i) s *= ext[i];
+        return s;
+    }
+};
+
+// Device-side decomposition: offset of linear index `idx` in tensor `t`.
+__host__ __device__ inline int64_t group_offset(const ModeGroup &g, int t, int64_t idx) {
+    int64_t off = 0;
+    for (int i = 0; i < g.n; ++i) {
+        int64_t e = g.ext[i];
+        int64_t q = idx / e;
+        off += (idx - q * e) * g.str[t][i];
+        idx = q;
+    }
+    return off;
+}
+
+// Internal tensor description with owned arrays.
+struct Desc {
+    int dtype = MGB_F64;
+    int rank = 0;
+    int32_t modes[kMaxRank];
+    int64_t ext[kMaxRank];
+    int64_t str[kMaxRank];
+};
+int read_desc(const mgb_tensor_desc *d, Desc &out, const char *name);
+
+enum class PlanKind { Contraction, Unary };
+
+// Resolved binary contraction: GEMM view C[l][m][n] = sum_k A[l][m][k] B[l][k][n].
+struct ContractionPlan {
+    Desc a, b, c;
+    int compute_dtype = MGB_F64;
+    int form = MGB_FORM_PLAIN;
+    int slices = 0;
+    // Groups: tensor index 0 = A, 1 = B, 2 = C.
+    ModeGroup gm, gn, gk, gl;
+    int64_t M = 1, N = 1, K = 1, L = 1;
+    // Plain form: operands of a different element type than the compute type
+    // are converted into the workspace first (dense, same mode order).
+    bool convert_a = false, convert_b = false;
+    // Ozaki / bf16x3 parameters.
+    int oz_w = 7;          // slice width in bits
+    int oz_kc = 256;       // k-chunk (embedded elements) between exact readouts
+    int oz_R = 0;          // -1 when K is too long for the exact accumulator
+    uint64_t ws_bytes = 0;
+    // workspace layout (byte offsets)
+    uint64_t ws_a = 0, ws_b = 0, ws_scale_a = 0, ws_scale_b = 0;
+    int64_t kpad = 0;      // padded embedded K of the slice buffers
+    int64_t m_e = 0, n_e = 0, k_e = 0;  // embedded GEMM extents
+};
+
+struct UnaryPlan {
+    Desc x, y;
+    ModeGroup go;  // output modes: tensor 0 = X stride, 1 = Y stride
+    ModeGroup gr;  // reduced modes: tensor 0 = X stride
+    int64_t O = 1, R = 1;
+};
+
+}  // namespace mgb
+
+struct mgb_plan_s {
+    mgb::PlanKind kind;
+    mgb::ContractionPlan cp;
+    mgb::UnaryPlan up;
+    // optional phase timing (mgb_plan_set_timing)
+    bool timing = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    ~mgb_plan_s() {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+namespace mgb {
+// Kernel launchers (each returns an mgb_status).
+int launch_permute(const Desc &x, const Desc &y, const void *X, void *Y, cudaStream_t s);
+int launch_fill_zero(void *p, int64_t count, int dtype, const Desc &d, cudaStream_t s);
+int launch_plain_gemm(const ContractionPlan &p, const void *A, const void *B, void *C,
+                      cudaStream_t s);
+int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C,
+                 void *ws, cudaStream_t s, cudaEvent_t mid = nullptr);
+int launch_unary(const UnaryPlan &p, const void *X, void *Y, cudaStream_t s);
+int32_t *device_status_ptr();  // per-device status word
+uint64_t ozaki_workspace(ContractionPlan &p);
+void ozaki_setup(ContractionPlan &p);
+}  // namespace mgb

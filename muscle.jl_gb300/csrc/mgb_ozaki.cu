@@ -1,0 +1,880 @@
+// Emulated forms on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// OZAKI (Float64 / ComplexF64 results)
+//   Each row m of A and column n of B gets a power-of-two scale from its
+//   largest exponent; the scaled value a in [-1, 1] is cut into S signed
+//   W-bit digits by round-to-nearest:  a = sum_i s_i 2^(-W i) + r,
+//   |s_1| <= 2^W, |s_i| <= 2^(W-1), |r| <= 2^(-W S - 1).  With W = 7 every
+//   digit is an integer that bf16 holds exactly, every digit product is
+//   exact, and a float32 accumulator stays exact while the sum of the
+//   absolute products it receives is <= 2^24.  Products s_i t_j with
+//   i + j = d share the scale 2^(-W d) and go to one TMEM accumulator per d
+//   ("group"); pairs with i + j > S + 1 are dropped (Ozaki scheme I).
+//   Every KC = 256 embedded k the epilogue warps read each group's float32
+//   partial sums (exact integers), convert them to int and add them, shifted
+//   left by W (S + 1 - d), into one exact 96-bit integer per output element
+//   (|X| < 2^(log2 K + W (S + 1) + 1) < 2^95 for any K below 2^31). The only
+//   float64 arithmetic left is the conversion of X and one ldexp per output
+//   element (GB300's FP64 pipe is slow).
+//   Group bound per k: max(d + 1, 4) * 2^(2W-2); KC * bound <= 2^24 for
+//   d <= 15, so the readout is exact for every S <= 8 supported here.
+//
+// BF16X3 (Float32 / ComplexF32 results)
+//   x = hi + mid + lo, three bf16 pieces; the six products with
+//   piece-index sum <= 4 accumulate in one float32 TMEM accumulator.
+//
+// Complex operands are embedded as real GEMMs: A_e[m][2k+p] = part_p(A[m,k]),
+// B_e[2n+q][2k+p] holds [[Br, -Bi], [Bi, Br]] so that C_e[m][2n+q] is part q
+// of C[m,n] (4 real products per complex product, as zgemm's 4M form).
+//
+// Pipeline per CTA (128 x 64 embedded outputs, one CTA per SM):
+//   warp 0       TMA producer: one 3-D box per operand per 32-wide k block
+//                loads all S slices at once into a 64B-swizzled stage;
+//   warp 1       TMEM allocation, then a single thread issues
+//                tcgen05.mma.cta_group::1.kind::f16 (M=128, N=64, K=16);
+//   warps 2..9   epilogue: tcgen05.ld 32x32b.x32 per group and column half.
+// Every mbarrier wait is bounded; on timeout the CTA records
+// MGB_ERR_DEVICE_TIMEOUT in the device status word, drains its copies and
+// MMAs, frees TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+
+#include "mgb_internal.h"
+
+namespace mgb {
+
+constexpr int OZ_W = 7;        // digit width (bits)
+constexpr int OZ_KC = 256;     // embedded k between exact readouts
+constexpr int OZ_BM = 128;     // rows of A per CTA (TMEM lanes)
+constexpr int OZ_BN = 64;      // embedded rows of B per CTA
+constexpr int OZ_BK = 32;      // k per stage (64-byte swizzled rows)
+constexpr int OZ_EPI_WARPS = 8;
+constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;
+constexpr int OZ_A_TILE = OZ_BM * OZ_BK * 2;  // 8192 bytes per slice
+constexpr int OZ_B_TILE = OZ_BN * OZ_BK * 2;  // 4096 bytes per slice
+constexpr int OZ_SMEM_BUDGET = 200 * 1024;
+constexpr long long OZ_TIMEOUT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
+
+__host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (OZ_A_TILE + OZ_B_TILE); }
+__host__ __device__ constexpr int oz_stages(int S) {
+    return (OZ_SMEM_BUDGET / oz_stage_bytes(S)) < 4 ? (OZ_SMEM_BUDGET / oz_stage_bytes(S)) : 4;
+}
+__host__ __device__ constexpr int oz_tmem_cols(int ng) {
+    return ng * OZ_BN <= 64 ? 64 : ng * OZ_BN <= 128 ? 128 : ng * OZ_BN <= 256 ? 256 : 512;
+}
+__host__ __device__ constexpr int oz_smem_bytes(int S) {
+    return oz_stages(S) * oz_stage_bytes(S) + 1024 /*align*/ + 512 /*barriers*/;
+}
+
+// =============================================================================
+// PTX wrappers
+// =============================================================================
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false when the CTA aborted or this wait timed out.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                          int32_t *status) {
+    if (mbar_try(bar, parity)) return true;
+    long long t0 = clock64();
+    while (true) {
+        if (mbar_try(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (clock64() - t0 > OZ_TIMEOUT_CYCLES) {
+            *abort_flag = 1;
+            atomicCAS(status, 0, (int32_t)MGB_ERR_DEVICE_TIMEOUT);
+            return false;
+        }
+    }
+}
+// Drain wait used after an abort: bounded, never raises the abort flag.
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+    long long t0 = clock64();
+    while (!mbar_try(bar, parity))
+        if (clock64() - t0 > OZ_TIMEOUT_CYCLES) return;
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *tm, int c0, int c1,
+                                            int c2, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+          "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+          "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+          "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// 96-bit two's-complement accumulation (carry chain) and conversion.
+__device__ __forceinline__ void add96(uint32_t &w0, uint32_t &w1, uint32_t &w2, uint32_t a0, uint32_t a1,
+                                      uint32_t a2) {
+    asm("add.cc.u32 %0, %0, %3;\n\taddc.cc.u32 %1, %1, %4;\n\taddc.u32 %2, %2, %5;"
+        : "+r"(w0), "+r"(w1), "+r"(w2)
+        : "r"(a0), "r"(a1), "r"(a2));
+}
+__device__ __forceinline__ void add64hi(uint32_t &w1, uint32_t &w2, uint32_t a1, uint32_t a2) {
+    asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(w1), "+r"(w2) : "r"(a1), "r"(a2));
+}
+__device__ __forceinline__ double x96_to_double(uint32_t w0, uint32_t w1, uint32_t w2) {
+    int64_t hi = (int64_t)(((uint64_t)w2 << 32) | w1);  // X = hi * 2^32 + w0
+    return fma(__ll2double_rn(hi), 4294967296.0, __uint2double_rn(w0));
+}
+
+// K-major operand tile, 64-byte swizzle: rows of 64 B, 8-row atoms of 512 B.
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);  // start address
+    d |= (uint64_t)1 << 16;                   // leading byte offset (unused here)
+    d |= (uint64_t)(512 >> 4) << 32;          // stride byte offset: 8 rows x 64 B
+    d |= (uint64_t)1 << 46;                   // descriptor version (sm_100 family)
+    d |= (uint64_t)4 << 61;                   // swizzle mode: 64 B
+    return d;
+}
+// kind::f16 instruction descriptor: f32 accumulate, bf16 A and B, both K-major.
+__host__ __device__ constexpr uint32_t oz_idesc() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
+           ((uint32_t)(OZ_BM >> 4) << 24);
+}
+
+// =============================================================================
+// Pre-pass 1: largest biased exponent per row of an operand
+// =============================================================================
+struct OpGeom {
+    ModeGroup gr, gk, gl;  // rows, contracted, batch
+    int t;                 // tensor index inside the groups (0 = A, 1 = B)
+    int64_t R, K;
+    int rows_fast;         // operand's unit-stride mode is a row mode
+};
+
+__device__ __forceinline__ int bexp(double v) {
+    return (int)((__double_as_longlong(v) >> 52) & 0x7FF);
+}
+__device__ __forceinline__ int bexp_of(double v) { return bexp(v); }
+__device__ __forceinline__ int bexp_of(double2 v) { return max(bexp(v.x), bexp(v.y)); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps) {
+    __shared__ int64_t roff[32], koff[32];
+    __shared__ int red[8][33];
+    int64_t tiles_k = (g.K + 31) / 32;
+    int64_t tr = blockIdx.x / tiles_k, tk = blockIdx.x - tr * tiles_k;
+    int64_t l = blockIdx.y;
+    int64_t r0 = tr * 32, k0 = tk * 32;
+    int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
+    if (tid < 32) roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
+    else if (tid < 64) koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
+    const T *Xl = X + group_offset(g.gl, g.t, l);
+    __syncthreads();
+    if (g.rows_fast) {
+        int e = 0;
+        int64_t r = r0 + tx;
+        for (int kk = ty; kk < 32; kk += 8)
+            if (r < g.R && k0 + kk < g.K) e = max(e, bexp_of(__ldg(Xl + roff[tx] + koff[kk])));
+        red[ty][tx] = e;
+    } else {
+        for (int j = 0; j < 4; ++j) {
+            int rr = ty + 8 * j;
+            int e = 0;
+            if (r0 + rr < g.R && k0 + tx < g.K) e = bexp_of(__ldg(Xl + roff[rr] + koff[tx]));
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, d));
+            if (tx == 0) red[j][rr] = e;  // rows rr = ty + 8 j are distinct per (ty, j)
+        }
+    }
+    __syncthreads();
+    if (tid < 32 && r0 + tid < g.R) {
+        int e = 0;
+        if (g.rows_fast) {
+            for (int j = 0; j < 8; ++j) e = max(e, red[j][tid]);
+        } else {
+            e = red[tid / 8 % 4][tid];  // written by ty = tid % 8, j = tid / 8
+        }
+        if (e > 0) atomicMax(exps + l * g.R + r0 + tid, e);
+    }
+}
+
+// =============================================================================
+// Pre-pass 2: slices (OZAKI digits or BF16X3 pieces), permutation fused
+// =============================================================================
+// Output words (2 x bf16) of slice plane s: out[((l*S + s) * rows_e + row) * kw + word].
+//   MODE_REAL : row = r,        word w holds k = 2w, 2w+1
+//   MODE_CA   : row = r,        word k holds (re, im)           (A side)
+//   MODE_CB   : rows 2r, 2r+1,  word k holds (re, -im), (im, re) (B side)
+enum { MODE_REAL = 0, MODE_CA = 1, MODE_CB = 2 };
+
+__device__ __forceinline__ uint32_t bf16_bits_of_int(int d) {
+    float f = __int_as_float(0x4B400000 + d) - 12582912.0f;  // exact for |d| < 2^22
+    return __float_as_uint(f) >> 16;                         // exact in bf16 for |d| <= 256
+}
+__device__ __forceinline__ uint32_t pack2(uint32_t lo, uint32_t hi) { return lo | (hi << 16); }
+
+// Signed round-to-nearest digits of x * 2^(-e) in 62-bit fixed point.
+__device__ __forceinline__ void oz_digits(double x, int e, int S, int (&d)[8]) {
+    uint64_t b = (uint64_t)__double_as_longlong(x);
+    int be = (int)((b >> 52) & 0x7FF);
+    int64_t m = (int64_t)(b & 0xFFFFFFFFFFFFFull);
+    int ex;
+    if (be) {
+        m |= (int64_t)1 << 52;
+        ex = be - 1075;
+    } else {
+        ex = -1074;
+    }
+    int sh = ex + 62 - e;  // Q = m * 2^sh < 2^62
+    int64_t Q;
+    if (sh >= 0) Q = m << sh;
+    else if (sh > -63) Q = m >> (-sh);
+    else Q = 0;
+    if (b >> 63) Q = -Q;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        int shift = 62 - OZ_W * (s + 1);
+        int64_t dig = (Q + ((int64_t)1 << (shift - 1))) >> shift;
+        Q -= dig << shift;
+        d[s] = s < S ? (int)dig : 0;
+    }
+}
+
+// Three bf16 pieces of a float: x = hi + mid + lo (to ~2^-24 relative).
+__device__ __forceinline__ void bf3_pieces(float x, uint32_t (&p)[8]) {
+    __nv_bfloat16 h = __float2bfloat16_rn(x);
+    float r = x - __bfloat162float(h);
+    __nv_bfloat16 m = __float2bfloat16_rn(r);
+    r = r - __bfloat162float(m);
+    __nv_bfloat16 l = __float2bfloat16_rn(r);
+    p[0] = __bfloat16_as_ushort(h);
+    p[1] = __bfloat16_as_ushort(m);
+    p[2] = __bfloat16_as_ushort(l);
+}
+
+template <typename T>
+struct OzIn;
+template <>
+struct OzIn<double> {
+    static constexpr bool cx = false;
+    __device__ static double re(double v) { return v; }
+    __device__ static double im(double) { return 0.0; }
+};
+template <>
+struct OzIn<double2> {
+    static constexpr bool cx = true;
+    __device__ static double re(double2 v) { return v.x; }
+    __device__ static double im(double2 v) { return v.y; }
+};
+template <>
+struct OzIn<float> {
+    static constexpr bool cx = false;
+    __device__ static float re(float v) { return v; }
+    __device__ static float im(float) { return 0.f; }
+};
+template <>
+struct OzIn<float2> {
+    static constexpr bool cx = true;
+    __device__ static float re(float2 v) { return v.x; }
+    __device__ static float im(float2 v) { return v.y; }
+};
+
+// BF3 = true: float inputs split into bf16 pieces; otherwise Ozaki digits.
+template <typename T, int MODE, bool BF3>
+__global__ void __launch_bounds__(256) k_oz_slice(const T *__restrict__ X, OpGeom g,
+                                                  const int32_t *__restrict__ exps, int S,
+                                                  uint32_t *__restrict__ out, int64_t rows_e,
+                                                  int64_t kw) {
+    constexpr int KT = MODE == MODE_REAL ? 64 : 32;  // k per tile
+    __shared__ T tile[32][KT + 1];
+    __shared__ int64_t roff[32], koff[KT];
+    __shared__ int rexp[32];
+    int64_t tiles_k = (g.K + KT - 1) / KT;
+    int64_t tr = blockIdx.x / tiles_k, tk = blockIdx.x - tr * tiles_k;
+    int64_t l = blockIdx.y;
+    int64_t r0 = tr * 32, k0 = tk * KT;
+    int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
+    if (tid < 32) {
+        roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
+        if (!BF3) {
+            int be = (r0 + tid < g.R) ? exps[l * g.R + r0 + tid] : 0;
+            rexp[tid] = be == 0x7FF ? 0x7FFFFFFF : (be == 0 ? -1022 : be - 1022);
+        }
+    }
+    if (tid < KT) koff[tid] = (k0 + tid < g.K) ? group_offset(g.gk, g.t, k0 + tid) : 0;
+    const T *Xl = X + group_offset(g.gl, g.t, l);
+    __syncthreads();
+    for (int idx = tid; idx < 32 * KT; idx += 256) {
+        int r, kk;
+        if (g.rows_fast) {
+            r = idx % 32;
+            kk = idx / 32;
+        } else {
+            kk = idx % KT;
+            r = idx / KT;
+        }
+        T v;
+        memset(&v, 0, sizeof(T));
+        if (r0 + r < g.R && k0 + kk < g.K) v = __ldg(Xl + roff[r] + koff[kk]);
+        tile[r][kk] = v;
+    }
+    __syncthreads();
+    const int64_t plane = rows_e * kw;
+    uint32_t *outl = out + l * (int64_t)S * plane;
+    for (int j = 0; j < 4; ++j) {
+        int r = ty + 8 * j;
+        int64_t row = r0 + r;
+        if (row >= g.R) continue;
+        int e = BF3 ? 0 : rexp[r];
+        bool bad = !BF3 && e == 0x7FFFFFFF;
+        if (MODE == MODE_REAL) {
+            int64_t word = k0 / 2 + tx;
+            if (word >= kw) continue;
+            uint32_t p0[8], p1[8];
+            if (BF3) {
+                bf3_pieces((float)OzIn<T>::re(tile[r][2 * tx]), p0);
+                bf3_pieces((float)OzIn<T>::re(tile[r][2 * tx + 1]), p1);
+            } else {
+                int d0[8], d1[8];
+                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx]), bad ? 0 : e, S, d0);
+                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx + 1]), bad ? 0 : e, S, d1);
+#pragma unroll
+                for (int s = 0; s < 8; ++s) {
+                    p0[s] = bf16_bits_of_int(d0[s]);
+                    p1[s] = bf16_bits_of_int(d1[s]);
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < 8; ++s)
+                if (s < S) outl[s * plane + row * kw + word] = pack2(p0[s], p1[s]);
+        } else {
+            int64_t word = k0 + tx;
+            if (word >= kw) continue;
+            uint32_t pr[8], pi[8], pn[8];
+            if (BF3) {
+                bf3_pieces((float)OzIn<T>::re(tile[r][tx]), pr);
+                bf3_pieces((float)OzIn<T>::im(tile[r][tx]), pi);
+                float nim = -(float)OzIn<T>::im(tile[r][tx]);
+                bf3_pieces(nim, pn);
+            } else {
+                int dr[8], di[8];
+                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][tx]), bad ? 0 : e, S, dr);
+                oz_digits(bad ? 0.0 : (double)OzIn<T>::im(tile[r][tx]), bad ? 0 : e, S, di);
+#pragma unroll
+                for (int s = 0; s < 8; ++s) {
+                    pr[s] = bf16_bits_of_int(dr[s]);
+                    pi[s] = bf16_bits_of_int(di[s]);
+                    pn[s] = bf16_bits_of_int(-di[s]);
+                }
+            }
+            if (MODE == MODE_CA) {
+#pragma unroll
+                for (int s = 0; s < 8; ++s)
+                    if (s < S) outl[s * plane + row * kw + word] = pack2(pr[s], pi[s]);
+            } else {
+#pragma unroll
+                for (int s = 0; s < 8; ++s)
+                    if (s < S) {
+                        outl[s * plane + (2 * row) * kw + word] = pack2(pr[s], pn[s]);
+                        outl[s * plane + (2 * row + 1) * kw + word] = pack2(pi[s], pr[s]);
+                    }
+            }
+        }
+    }
+}
+
+// =============================================================================
+// The tcgen05 GEMM over slices
+// =============================================================================
+struct OzGemmArgs {
+    int64_t M, Ne, N;      // rows of A, embedded rows of B, un-embedded N
+    int32_t nkb;           // number of 32-wide k blocks
+    int32_t kcb;           // k blocks per exact chunk
+    int32_t S;             // slices (digits / pieces)
+    const int32_t *expA;   // [L][M] biased exponents (OZAKI)
+    const int32_t *expB;   // [L][N]
+    void *C;
+    ModeGroup gm, gn, gl;  // C offsets live in tensor slot 2
+    int32_t *status;
+};
+
+template <int S, bool EXACT, bool CX>
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    k_oz_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+              const OzGemmArgs args) {
+    constexpr int NG = EXACT ? S : 1;
+    constexpr int NST = oz_stages(S);
+    constexpr int STAGE = oz_stage_bytes(S);
+    constexpr int TCOLS = oz_tmem_cols(NG);
+    static_assert(NST >= 2, "need at least two pipeline stages");
+    static_assert(NG * OZ_BN <= 512, "TMEM holds at most 512 columns");
+
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + NST * STAGE);
+    uint64_t *full = bars;              // [NST]
+    uint64_t *empty = bars + NST;       // [NST]
+    uint64_t *acc_full = bars + 2 * NST;
+    uint64_t *acc_empty = bars + 2 * NST + 1;  // [NG]
+    uint64_t *done = bars + 2 * NST + 1 + NG;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    const int64_t n0 = (int64_t)blockIdx.x * OZ_BN, m0 = (int64_t)blockIdx.y * OZ_BM;
+    const int l = blockIdx.z;
+
+    if (tid == 0) {
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(smem_u32(full + s), 1);
+            mbar_init(smem_u32(empty + s), 1);
+        }
+        mbar_init(smem_u32(acc_full), 1);
+        for (int g = 0; g < NG; ++g) mbar_init(smem_u32(acc_empty + g), OZ_EPI_WARPS);
+        mbar_init(smem_u32(done), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"((uint32_t)TCOLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int nkb = args.nkb, kcb = args.kcb;
+    const int nchunks = (nkb + kcb - 1) / kcb;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            int issued = 0;
+            for (int kb = 0; kb < nkb; ++kb) {
+                int s = kb % NST;
+                uint32_t round = kb / NST;
+                if (!mbar_wait(smem_u32(empty + s), (round & 1) ^ 1, abort_flag, args.status)) break;
+                uint8_t *st = smem + s * STAGE;
+                mbar_expect_tx(smem_u32(full + s), STAGE);
+                tma_load_3d(smem_u32(st), &tmA, kb * OZ_BK, (int)m0, l * S, smem_u32(full + s));
+                tma_load_3d(smem_u32(st + S * OZ_A_TILE), &tmB, kb * OZ_BK, (int)n0, l * S,
+                            smem_u32(full + s));
+                issued = kb + 1;
+            }
+            // make sure no bulk copy is still writing into shared memory
+            for (int kb = max(0, issued - NST); kb < issued; ++kb)
+                mbar_drain(smem_u32(full + kb % NST), (kb / NST) & 1);
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            const uint32_t idesc = oz_idesc();
+            int chunk = 0;
+            uint32_t touched = 0;
+            bool ok = true;
+            for (int kb = 0; kb < nkb && ok; ++kb) {
+                int s = kb % NST;
+                uint32_t round = kb / NST;
+                bool chunk_start = (kb % kcb) == 0;
+                if (!mbar_wait(smem_u32(full + s), round & 1, abort_flag, args.status)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a_base = smem_u32(smem + s * STAGE);
+                const uint32_t b_base = a_base + S * OZ_A_TILE;
+#pragma unroll
+                for (int k16 = 0; k16 < OZ_BK / 16; ++k16) {
+#pragma unroll
+                    for (int i = 0; i < S; ++i) {
+#pragma unroll
+                        for (int j = 0; j < S - i; ++j) {
+                            const int g = EXACT ? i + j : 0;
+                            const bool first = chunk_start && k16 == 0 && !(touched & (1u << g));
+                            if (first && ok) {
+                                // group g of the previous chunk must have been read out
+                                ok = mbar_wait(smem_u32(acc_empty + g), (chunk & 1) ^ 1, abort_flag,
+                                               args.status);
+                                tc_fence_after();
+                                touched |= 1u << g;
+                            }
+                            if (ok) {
+                                uint64_t ad = sw64_desc(a_base + i * OZ_A_TILE + k16 * 32);
+                                uint64_t bd = sw64_desc(b_base + j * OZ_B_TILE + k16 * 32);
+                                tc_mma(tmem + g * OZ_BN, ad, bd, idesc, first ? 0u : 1u);
+                            }
+                        }
+                    }
+                }
+                if (!ok) break;
+                tc_commit(smem_u32(empty + s));
+                if ((kb % kcb) == kcb - 1 || kb == nkb - 1) {
+                    tc_commit(smem_u32(acc_full));
+                    ++chunk;
+                    touched = 0;
+                }
+            }
+            // wait for every MMA this thread issued before TMEM is released
+            tc_commit(smem_u32(done));
+            mbar_drain(smem_u32(done), 0);
+        }
+    } else {
+        // ---------------- epilogue ----------------
+        const int q = warp % 4;           // TMEM lane quarter this warp may access
+        const int h = (warp - 2) / 4;     // column half of each group
+        const int64_t row = m0 + 32 * q + lane;
+        const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + 32 * h;
+        // EXACT: one 96-bit two's-complement integer per output column,
+        // X = sum_d G_d 2^(W (S + 1 - d)), held in w0 (bits 0-31), w1, w2.
+        uint32_t w0[EXACT ? 32 : 1], w1[EXACT ? 32 : 1], w2[EXACT ? 32 : 1];
+        float accf[EXACT ? 1 : 32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            if (EXACT) {
+                w0[j] = 0;
+                w1[j] = 0;
+                w2[j] = 0;
+            } else {
+                accf[j] = 0.f;
+            }
+        }
+        bool ok = true;
+        for (int c = 0; c < nchunks && ok; ++c) {
+            if (!mbar_wait(smem_u32(acc_full), c & 1, abort_flag, args.status)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+#pragma unroll 1
+            for (int g = 0; g < NG; ++g) {
+                uint32_t v[32];
+                tc_ld32(tbase + g * OZ_BN, v);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(acc_empty + g));
+                if (EXACT) {
+                    const int sh = OZ_W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
+                    if (sh < 32) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
+                            add96(w0[j], w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32),
+                                  t < 0 ? 0xFFFFFFFFu : 0u);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
+                            add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) accf[j] += __uint_as_float(v[j]);
+                }
+            }
+        }
+        if (ok && row < args.M) {
+            const int64_t lb = group_offset(args.gl, 2, l);
+            const int64_t om = group_offset(args.gm, 2, row);
+            int erow = 0;
+            bool badrow = false;
+            if (EXACT) {
+                int be = args.expA[(int64_t)l * args.M + row];
+                badrow = be == 0x7FF;
+                erow = be == 0 ? -1022 : be - 1022;
+            }
+#pragma unroll
+            for (int j = 0; j < 32; j += (CX ? 2 : 1)) {
+                int64_t ne = n0 + 32 * h + j;
+                if (ne >= args.Ne) continue;
+                int64_t n = CX ? (ne >> 1) : ne;
+                int64_t off = lb + om + group_offset(args.gn, 2, n);
+                if (EXACT) {
+                    int bc = args.expB[(int64_t)l * args.N + n];
+                    bool bad = badrow || bc == 0x7FF;
+                    int ecol = bc == 0 ? -1022 : bc - 1022;
+                    const int E = erow + ecol - OZ_W * (S + 1);
+                    const double nan = __longlong_as_double(0x7FF8000000000000LL);
+                    double v0 = bad ? nan : ldexp(x96_to_double(w0[j], w1[j], w2[j]), E);
+                    if (CX) {
+                        double v1 = bad ? nan : ldexp(x96_to_double(w0[j + 1], w1[j + 1], w2[j + 1]), E);
+                        ((double2 *)args.C)[off] = make_double2(v0, v1);
+                    } else {
+                        ((double *)args.C)[off] = v0;
+                    }
+                } else {
+                    if (CX) ((float2 *)args.C)[off] = make_float2(accf[j], accf[j + 1]);
+                    else ((float *)args.C)[off] = accf[j];
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"((uint32_t)TCOLS)
+                     : "memory");
+}
+
+// =============================================================================
+// Host side
+// =============================================================================
+static uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
+
+void ozaki_setup(ContractionPlan &p) {
+    bool cx = is_complex(p.compute_dtype);
+    int S = p.slices;
+    p.m_e = p.M;
+    p.n_e = cx ? 2 * p.N : p.N;
+    p.k_e = cx ? 2 * p.K : p.K;
+    p.kpad = (p.k_e + 7) / 8 * 8;
+    p.oz_w = OZ_W;
+    p.oz_kc = OZ_KC;
+    uint64_t off = 0;
+    p.ws_a = off;
+    off = align256(off + (uint64_t)p.L * S * p.m_e * p.kpad * 2);
+    p.ws_b = off;
+    off = align256(off + (uint64_t)p.L * S * p.n_e * p.kpad * 2);
+    if (p.form == MGB_FORM_OZAKI) {
+        p.ws_scale_a = off;
+        off = align256(off + (uint64_t)p.L * p.M * 4);
+        p.ws_scale_b = off;
+        off = align256(off + (uint64_t)p.L * p.N * 4);
+        // |X| <= k_e * 2^(2W) * 2^(W(S-1)) * (1 + small) must stay below 2^95
+        double xb = std::log2((double)std::max<int64_t>(p.k_e, 1)) + 2 * OZ_W + OZ_W * (S - 1) + 1;
+        p.oz_R = xb < 94 ? 0 : -1;  // -1: K too long for the exact accumulator
+    }
+    p.ws_bytes = off;
+}
+
+typedef CUresult (*PFN_encodeTiled_t)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                      const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                      const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                      CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static PFN_encodeTiled_t encode_fn() {
+    static PFN_encodeTiled_t fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_encodeTiled_t)p;
+    });
+    return fn;
+}
+
+static int make_map(CUtensorMap *tm, void *base, int64_t k_e, int64_t rows, int64_t planes,
+                    int64_t kpad, int box_rows, int S) {
+    PFN_encodeTiled_t enc = encode_fn();
+    if (!enc) return fail(MGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[3] = {(cuuint64_t)k_e, (cuuint64_t)rows, (cuuint64_t)planes};
+    cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)(kpad * 2 * rows)};
+    cuuint32_t box[3] = {OZ_BK, (cuuint32_t)box_rows, (cuuint32_t)S};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return fail(MGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return MGB_OK;
+}
+
+template <int S, bool EXACT, bool CX>
+static int launch_gemm_t(const CUtensorMap &ta, const CUtensorMap &tb, const OzGemmArgs &a, dim3 grid,
+                         cudaStream_t s) {
+    auto kern = k_oz_gemm<S, EXACT, CX>;
+    constexpr int smem = oz_smem_bytes(S);
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!attr_set[dev & 63]) {
+        MGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr_set[dev & 63] = true;
+    }
+    kern<<<grid, OZ_THREADS, smem, s>>>(ta, tb, a);
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
+}
+
+static int launch_gemm(int S, bool exact, bool cx, const CUtensorMap &ta, const CUtensorMap &tb,
+                       const OzGemmArgs &a, dim3 grid, cudaStream_t s) {
+    if (!exact) return cx ? launch_gemm_t<3, false, true>(ta, tb, a, grid, s)
+                          : launch_gemm_t<3, false, false>(ta, tb, a, grid, s);
+#define OZ_CASE(SS)                                                                  \
+    case SS:                                                                         \
+        return cx ? launch_gemm_t<SS, true, true>(ta, tb, a, grid, s)                \
+                  : launch_gemm_t<SS, true, false>(ta, tb, a, grid, s);
+    switch (S) {
+        OZ_CASE(3)
+        OZ_CASE(4)
+        OZ_CASE(5)
+        OZ_CASE(6)
+        OZ_CASE(7)
+        OZ_CASE(8)
+    }
+#undef OZ_CASE
+    return fail(MGB_ERR_ARGUMENT, "unsupported slice count");
+}
+
+static int unit_row_fast(const ModeGroup &gr, const ModeGroup &gk, int t) {
+    int64_t sr = gr.n > 0 ? std::llabs(gr.str[t][0]) : INT64_MAX;
+    int64_t sk = gk.n > 0 ? std::llabs(gk.str[t][0]) : INT64_MAX;
+    return sr <= sk ? 1 : 0;
+}
+
+template <typename T, bool BF3>
+static int run_prepass(const OpGeom &g, int mode, const void *X, int32_t *exps, int S, uint32_t *out,
+                       int64_t rows_e, int64_t kw, int64_t L, cudaStream_t s) {
+    int KT = mode == MODE_REAL ? 64 : 32;
+    int64_t tiles = ((g.R + 31) / 32) * ((g.K + KT - 1) / KT);
+    if (tiles > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the slicer grid");
+    dim3 grid((unsigned)tiles, (unsigned)L);
+    const T *x = (const T *)X;
+    switch (mode) {
+    case MODE_REAL: k_oz_slice<T, MODE_REAL, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, out, rows_e, kw); break;
+    case MODE_CA: k_oz_slice<T, MODE_CA, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, out, rows_e, kw); break;
+    default: k_oz_slice<T, MODE_CB, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, out, rows_e, kw); break;
+    }
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
+}
+
+template <typename T>
+static int run_scale(const OpGeom &g, const void *X, int32_t *exps, int64_t L, cudaStream_t s) {
+    int64_t tiles = ((g.R + 31) / 32) * ((g.K + 31) / 32);
+    if (tiles > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the scale grid");
+    dim3 grid((unsigned)tiles, (unsigned)L);
+    k_oz_scale<T><<<grid, 256, 0, s>>>((const T *)X, g, exps);
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
+}
+
+int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C, void *ws,
+                 cudaStream_t s, cudaEvent_t mid) {
+    if (((uintptr_t)ws & 255) != 0) return fail(MGB_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+    const bool exact = p.form == MGB_FORM_OZAKI;
+    const bool cx = is_complex(p.compute_dtype);
+    const int S = p.slices;
+    uint8_t *w = (uint8_t *)ws;
+    uint32_t *sa = (uint32_t *)(w + p.ws_a), *sb = (uint32_t *)(w + p.ws_b);
+    int32_t *ea = exact ? (int32_t *)(w + p.ws_scale_a) : nullptr;
+    int32_t *eb = exact ? (int32_t *)(w + p.ws_scale_b) : nullptr;
+    int32_t *status = device_status_ptr();
+    if (!status) return fail(MGB_ERR_CUDA, "device status word unavailable");
+
+    OpGeom ga, gb;
+    ga.gr = p.gm; ga.gk = p.gk; ga.gl = p.gl; ga.t = 0; ga.R = p.M; ga.K = p.K;
+    ga.rows_fast = unit_row_fast(p.gm, p.gk, 0);
+    gb.gr = p.gn; gb.gk = p.gk; gb.gl = p.gl; gb.t = 1; gb.R = p.N; gb.K = p.K;
+    gb.rows_fast = unit_row_fast(p.gn, p.gk, 1);
+    const int64_t kw = p.kpad / 2;
+    const int mode_a = cx ? MODE_CA : MODE_REAL, mode_b = cx ? MODE_CB : MODE_REAL;
+    int st;
+    if (exact) {
+        MGB_CUDA_CHECK(cudaMemsetAsync(ea, 0, (size_t)p.L * p.M * 4, s));
+        MGB_CUDA_CHECK(cudaMemsetAsync(eb, 0, (size_t)p.L * p.N * 4, s));
+        st = p.a.dtype == MGB_C64 ? run_scale<double2>(ga, A, ea, p.L, s) : run_scale<double>(ga, A, ea, p.L, s);
+        if (st) return st;
+        st = p.b.dtype == MGB_C64 ? run_scale<double2>(gb, B, eb, p.L, s) : run_scale<double>(gb, B, eb, p.L, s);
+        if (st) return st;
+        st = p.a.dtype == MGB_C64 ? run_prepass<double2, false>(ga, mode_a, A, ea, S, sa, p.m_e, kw, p.L, s)
+                                  : run_prepass<double, false>(ga, mode_a, A, ea, S, sa, p.m_e, kw, p.L, s);
+        if (st) return st;
+        st = p.b.dtype == MGB_C64 ? run_prepass<double2, false>(gb, mode_b, B, eb, S, sb, p.n_e, kw, p.L, s)
+                                  : run_prepass<double, false>(gb, mode_b, B, eb, S, sb, p.n_e, kw, p.L, s);
+        if (st) return st;
+    } else {
+        st = p.a.dtype == MGB_C32 ? run_prepass<float2, true>(ga, mode_a, A, nullptr, 3, sa, p.m_e, kw, p.L, s)
+                                  : run_prepass<float, true>(ga, mode_a, A, nullptr, 3, sa, p.m_e, kw, p.L, s);
+        if (st) return st;
+        st = p.b.dtype == MGB_C32 ? run_prepass<float2, true>(gb, mode_b, B, nullptr, 3, sb, p.n_e, kw, p.L, s)
+                                  : run_prepass<float, true>(gb, mode_b, B, nullptr, 3, sb, p.n_e, kw, p.L, s);
+        if (st) return st;
+    }
+    if (mid) MGB_CUDA_CHECK(cudaEventRecord(mid, s));
+    CUtensorMap ta, tb;
+    if ((st = make_map(&ta, sa, p.k_e, p.m_e, p.L * S, p.kpad, OZ_BM, S))) return st;
+    if ((st = make_map(&tb, sb, p.k_e, p.n_e, p.L * S, p.kpad, OZ_BN, S))) return st;
+    OzGemmArgs a;
+    a.M = p.M;
+    a.Ne = p.n_e;
+    a.N = p.N;
+    a.nkb = (int32_t)((p.k_e + OZ_BK - 1) / OZ_BK);
+    a.kcb = exact ? OZ_KC / OZ_BK : a.nkb;
+    a.S = S;
+    a.expA = ea;
+    a.expB = eb;
+    a.C = C;
+    a.gm = p.gm;
+    a.gn = p.gn;
+    a.gl = p.gl;
+    a.status = status;
+    if (a.gm.n == 0) { a.gm.n = 1; a.gm.ext[0] = 1; for (int t = 0; t < 3; ++t) a.gm.str[t][0] = 0; }
+    if (a.gn.n == 0) { a.gn.n = 1; a.gn.ext[0] = 1; for (int t = 0; t < 3; ++t) a.gn.str[t][0] = 0; }
+    dim3 grid((unsigned)((p.n_e + OZ_BN - 1) / OZ_BN), (unsigned)((p.M + OZ_BM - 1) / OZ_BM),
+              (unsigned)p.L);
+    if ((p.M + OZ_BM - 1) / OZ_BM > 65535) return fail(MGB_ERR_UNSUPPORTED, "M too large for the grid");
+    return launch_gemm(S, exact, cx, ta, tb, a, grid, s);
+}
+
+}  // namespace mgb

@@ -1,0 +1,292 @@
+// Index permutation (Base.permutedims via src/Tensor.jl:316-319) with optional
+// widening element conversion (real -> complex, Float32 -> Float64).
+//
+// After folding, the copy is one of:
+//  * row copy   — the fastest mode of Y is also unit-stride in X: contiguous
+//                 rows, copied with 128-bit vectors when aligned;
+//  * transpose  — X and Y have different unit-stride modes: 32x32 (or 64x64
+//                 for 4-byte types) shared-memory tiles, coalesced on both
+//                 sides, other modes enumerated by the grid;
+//  * gather     — strided views without a unit-stride mode: element-wise.
+// HBM-bound: algorithmic bytes = numel * (sizeof(src) + sizeof(dst)).
+#include <algorithm>
+#include <cuComplex.h>
+#include <type_traits>
+
+#include "mgb_internal.h"
+
+namespace mgb {
+
+template <typename TS, typename TD>
+struct Conv;
+template <typename T>
+struct Conv<T, T> {
+    __device__ static T f(T v) { return v; }
+};
+template <>
+struct Conv<float, double> {
+    __device__ static double f(float v) { return (double)v; }
+};
+template <>
+struct Conv<float, float2> {
+    __device__ static float2 f(float v) { return make_float2(v, 0.f); }
+};
+template <>
+struct Conv<float, double2> {
+    __device__ static double2 f(float v) { return make_double2((double)v, 0.0); }
+};
+template <>
+struct Conv<double, double2> {
+    __device__ static double2 f(double v) { return make_double2(v, 0.0); }
+};
+template <>
+struct Conv<float2, double2> {
+    __device__ static double2 f(float2 v) { return make_double2((double)v.x, (double)v.y); }
+};
+
+struct PermGeom {
+    ModeGroup g;    // folded modes, tensor 0 = X, 1 = Y; mode 0 = Y's fastest
+    int a = -1;     // Y unit-stride mode (0) or -1
+    int b = -1;     // X unit-stride mode or -1
+};
+
+// ---- row copy --------------------------------------------------------------
+constexpr int kRowChunk = 4096;
+
+template <typename TS, typename TD>
+__global__ void k_rowcopy(const TS *__restrict__ x, TD *__restrict__ y, ModeGroup outer,
+                          int64_t rowlen, int64_t chunks_per_row, int vec) {
+    int64_t blk = blockIdx.x;
+    int64_t row = blk / chunks_per_row;
+    int64_t chunk = blk - row * chunks_per_row;
+    const TS *xr = x + group_offset(outer, 0, row);
+    TD *yr = y + group_offset(outer, 1, row);
+    int64_t begin = chunk * kRowChunk;
+    int64_t end = min(begin + (int64_t)kRowChunk, rowlen);
+    if (vec) {
+        // same type, 16-byte aligned rows: copy 16-byte vectors
+        constexpr int per = 16 / sizeof(TD);
+        const uint4 *xs = reinterpret_cast<const uint4 *>(xr + begin);
+        uint4 *ys = reinterpret_cast<uint4 *>(yr + begin);
+        int64_t nv = (end - begin) / per;
+        for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) ys[i] = __ldg(xs + i);
+        for (int64_t i = begin + nv * per + threadIdx.x; i < end; i += blockDim.x)
+            yr[i] = Conv<TS, TD>::f(xr[i]);
+        return;
+    }
+    for (int64_t i = begin + threadIdx.x; i < end; i += blockDim.x) yr[i] = Conv<TS, TD>::f(xr[i]);
+}
+
+// ---- tiled transpose ------------------------------------------------------------
+template <typename TS, typename TD, int T>
+__global__ void k_transpose(const TS *__restrict__ x, TD *__restrict__ y, ModeGroup outer,
+                            int64_t ea, int64_t eb, int64_t sxa, int64_t syb, int64_t tiles_a,
+                            int64_t tiles_b) {
+    __shared__ TD tile[T][T + 1];
+    int64_t blk = blockIdx.x;
+    int64_t tb = blk % tiles_b;
+    blk /= tiles_b;
+    int64_t ta = blk % tiles_a;
+    int64_t o = blk / tiles_a;
+    const TS *xo = x + group_offset(outer, 0, o);
+    TD *yo = y + group_offset(outer, 1, o);
+    int64_t a0 = ta * T, b0 = tb * T;
+    int tx = threadIdx.x % 32, ty = threadIdx.x / 32;  // 32 x 8
+#pragma unroll
+    for (int bb = 0; bb < T; bb += 32) {
+#pragma unroll 4
+        for (int r = ty; r < T; r += 8) {
+            int64_t ia = a0 + r, ib = b0 + bb + tx;
+            if (ia < ea && ib < eb) tile[r][bb + tx] = Conv<TS, TD>::f(__ldg(xo + ia * sxa + ib));
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int aa = 0; aa < T; aa += 32) {
+#pragma unroll 4
+        for (int r = ty; r < T; r += 8) {
+            int64_t ib = b0 + r, ia = a0 + aa + tx;
+            if (ia < ea && ib < eb) yo[ia + ib * syb] = tile[aa + tx][r];
+        }
+    }
+}
+
+// ---- gather (no unit-stride mode) ---------------------------------------------
+template <typename TS, typename TD>
+__global__ void k_gather(const TS *__restrict__ x, TD *__restrict__ y, ModeGroup g, int64_t total) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t idx = i, ox = 0, oy = 0;
+        for (int m = 0; m < g.n; ++m) {
+            int64_t e = g.ext[m];
+            int64_t q = idx / e;
+            int64_t r = idx - q * e;
+            ox += r * g.str[0][m];
+            oy += r * g.str[1][m];
+            idx = q;
+        }
+        y[oy] = Conv<TS, TD>::f(x[ox]);
+    }
+}
+
+static ModeGroup drop_mode(const ModeGroup &g, int a, int b) {
+    ModeGroup o;
+    o.n = 0;
+    for (int i = 0; i < g.n; ++i) {
+        if (i == a || i == b) continue;
+        o.ext[o.n] = g.ext[i];
+        for (int t = 0; t < 3; ++t) o.str[t][o.n] = g.str[t][i];
+        ++o.n;
+    }
+    return o;
+}
+
+template <typename TS, typename TD>
+static int run_permute(const PermGeom &pg, const TS *x, TD *y, cudaStream_t s) {
+    const ModeGroup &g = pg.g;
+    int64_t total = g.size();
+    if (total == 0) return MGB_OK;
+    if (pg.a == 0 && pg.b == 0) {
+        ModeGroup outer = drop_mode(g, 0, 0);
+        int64_t rowlen = g.ext[0];
+        int64_t nrows = outer.size();
+        int64_t cpr = (rowlen + kRowChunk - 1) / kRowChunk;
+        int vec = 0;
+        if (sizeof(TS) == sizeof(TD) && std::is_same<TS, TD>::value && sizeof(TD) <= 16) {
+            bool al = ((uintptr_t)x % 16 == 0) && ((uintptr_t)y % 16 == 0);
+            for (int i = 0; i < outer.n; ++i)
+                al = al && ((outer.str[0][i] * (int64_t)sizeof(TS)) % 16 == 0) &&
+                     ((outer.str[1][i] * (int64_t)sizeof(TD)) % 16 == 0);
+            al = al && ((kRowChunk * sizeof(TD)) % 16 == 0);
+            vec = al ? 1 : 0;
+        }
+        int64_t blocks = nrows * cpr;
+        if (blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "permute: too many rows");
+        k_rowcopy<TS, TD><<<(unsigned)blocks, 256, 0, s>>>(x, y, outer, rowlen, cpr, vec);
+    } else if (pg.a == 0 && pg.b > 0) {
+        ModeGroup outer = drop_mode(g, 0, pg.b);
+        int64_t ea = g.ext[0], eb = g.ext[pg.b];
+        int64_t sxa = g.str[0][0], syb = g.str[1][pg.b];
+        constexpr int T = sizeof(TD) <= 4 ? 64 : 32;
+        int64_t tiles_a = (ea + T - 1) / T, tiles_b = (eb + T - 1) / T;
+        int64_t blocks = tiles_a * tiles_b * outer.size();
+        if (blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "permute: too many tiles");
+        k_transpose<TS, TD, T><<<(unsigned)blocks, 256, 0, s>>>(x, y, outer, ea, eb, sxa, syb,
+                                                               tiles_a, tiles_b);
+    } else {
+        int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 32);
+        k_gather<TS, TD><<<(unsigned)blocks, 256, 0, s>>>(x, y, g, total);
+    }
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
+}
+
+int launch_permute(const Desc &x, const Desc &y, const void *X, void *Y, cudaStream_t s) {
+    // modes in Y's order with their X strides; fold with Y as the primary tensor
+    ModeGroup g;
+    g.n = 0;
+    bool empty = false;
+    struct R {
+        int64_t e, sx, sy;
+    };
+    std::vector<R> ms;
+    for (int i = 0; i < y.rank; ++i) {
+        int j = 0;
+        while (j < x.rank && x.modes[j] != y.modes[i]) ++j;
+        if (y.ext[i] == 0) empty = true;
+        if (y.ext[i] == 1) continue;
+        ms.push_back({y.ext[i], x.str[j], y.str[i]});
+    }
+    if (empty) return MGB_OK;
+    std::stable_sort(ms.begin(), ms.end(),
+                     [](const R &p, const R &q) { return std::llabs(p.sy) < std::llabs(q.sy); });
+    std::vector<R> f;
+    for (auto &m : ms) {
+        if (!f.empty() && m.sx == f.back().sx * f.back().e && m.sy == f.back().sy * f.back().e) {
+            f.back().e *= m.e;
+            continue;
+        }
+        f.push_back(m);
+    }
+    PermGeom pg;
+    g.n = (int)f.size();
+    for (int i = 0; i < g.n; ++i) {
+        g.ext[i] = f[i].e;
+        g.str[0][i] = f[i].sx;
+        g.str[1][i] = f[i].sy;
+        g.str[2][i] = 0;
+    }
+    if (g.n == 0) {  // single element
+        g.n = 1;
+        g.ext[0] = 1;
+        g.str[0][0] = g.str[1][0] = 1;
+        g.str[2][0] = 0;
+    }
+    pg.g = g;
+    if (g.str[1][0] == 1) pg.a = 0;
+    for (int i = 0; i < g.n; ++i)
+        if (g.str[0][i] == 1) {
+            pg.b = i;
+            break;
+        }
+    if (pg.a != 0) pg.b = -1;
+    if (pg.b < 0) pg.a = -1;
+
+#define MGB_PERM_CASE(SD, DD, TS, TD) \
+    if (x.dtype == SD && y.dtype == DD) return run_permute<TS, TD>(pg, (const TS *)X, (TD *)Y, s);
+    MGB_PERM_CASE(MGB_F32, MGB_F32, float, float)
+    MGB_PERM_CASE(MGB_F64, MGB_F64, double, double)
+    MGB_PERM_CASE(MGB_C32, MGB_C32, float2, float2)
+    MGB_PERM_CASE(MGB_C64, MGB_C64, double2, double2)
+    MGB_PERM_CASE(MGB_F32, MGB_F64, float, double)
+    MGB_PERM_CASE(MGB_F32, MGB_C32, float, float2)
+    MGB_PERM_CASE(MGB_F32, MGB_C64, float, double2)
+    MGB_PERM_CASE(MGB_F64, MGB_C64, double, double2)
+    MGB_PERM_CASE(MGB_C32, MGB_C64, float2, double2)
+#undef MGB_PERM_CASE
+    return fail(MGB_ERR_ARGUMENT, "permute: unsupported conversion");
+}
+
+// ---- zero fill for K == 0 contractions (sum over an empty range) ----------------
+template <typename T>
+__global__ void k_fill_zero(T *y, ModeGroup g, int64_t total) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t idx = i, off = 0;
+        for (int m = 0; m < g.n; ++m) {
+            int64_t e = g.ext[m];
+            int64_t q = idx / e;
+            off += (idx - q * e) * g.str[0][m];
+            idx = q;
+        }
+        T z;
+        memset(&z, 0, sizeof(T));
+        y[off] = z;
+    }
+}
+
+int launch_fill_zero(void *p, int64_t count, int dtype, const Desc &d, cudaStream_t s) {
+    ModeGroup g;
+    g.n = d.rank;
+    for (int i = 0; i < d.rank; ++i) {
+        g.ext[i] = d.ext[i];
+        g.str[0][i] = d.str[i];
+        g.str[1][i] = g.str[2][i] = 0;
+    }
+    if (g.n == 0) {
+        g.n = 1;
+        g.ext[0] = 1;
+        g.str[0][0] = 1;
+    }
+    int64_t blocks = std::min<int64_t>((count + 255) / 256, 152 * 16);
+    switch (dtype) {
+    case MGB_F32: k_fill_zero<float><<<(unsigned)blocks, 256, 0, s>>>((float *)p, g, count); break;
+    case MGB_F64: k_fill_zero<double><<<(unsigned)blocks, 256, 0, s>>>((double *)p, g, count); break;
+    case MGB_C32: k_fill_zero<float2><<<(unsigned)blocks, 256, 0, s>>>((float2 *)p, g, count); break;
+    default: k_fill_zero<double2><<<(unsigned)blocks, 256, 0, s>>>((double2 *)p, g, count); break;
+    }
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
+}
+
+}  // namespace mgb

@@ -1,0 +1,132 @@
+// unary_einsum: Y[out] = sum over the remaining labels of X, where a label
+// repeated in X walks the diagonal (src/Operations/unary_einsum.jl:26-46,
+// ext/MuscleOMEinsumExt.jl:25-38; cases pinned by
+// test/integration/omeinsum.jl:6-100: axis sum, full sum, ii->i, iji->ij,
+// ii->, iji->j). The plan folds each distinct label into one mode whose X
+// stride is the sum of its positions' strides, so the kernel is a strided
+// reduction: y(o) = sum_r x(off_o + off_r). Memory-bound.
+#include <algorithm>
+
+#include "mgb_internal.h"
+
+namespace mgb {
+
+template <typename T>
+struct Acc;
+template <>
+struct Acc<float> {
+    using V = float;
+    __device__ static V zero() { return 0.f; }
+    __device__ static V add(V a, V b) { return a + b; }
+};
+template <>
+struct Acc<double> {
+    using V = double;
+    __device__ static V zero() { return 0.0; }
+    __device__ static V add(V a, V b) { return a + b; }
+};
+template <>
+struct Acc<float2> {
+    using V = float2;
+    __device__ static V zero() { return make_float2(0.f, 0.f); }
+    __device__ static V add(V a, V b) { return make_float2(a.x + b.x, a.y + b.y); }
+};
+template <>
+struct Acc<double2> {
+    using V = double2;
+    __device__ static V zero() { return make_double2(0.0, 0.0); }
+    __device__ static V add(V a, V b) { return make_double2(a.x + b.x, a.y + b.y); }
+};
+
+template <typename T>
+__device__ __forceinline__ T shfl_down(T v, int d);
+template <>
+__device__ __forceinline__ float shfl_down(float v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
+template <>
+__device__ __forceinline__ double shfl_down(double v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
+template <>
+__device__ __forceinline__ float2 shfl_down(float2 v, int d) {
+    return make_float2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+template <>
+__device__ __forceinline__ double2 shfl_down(double2 v, int d) {
+    return make_double2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+
+// One thread per output (short reductions).
+template <typename T>
+__global__ void k_unary_thread(const T *__restrict__ x, T *__restrict__ y, ModeGroup go, ModeGroup gr,
+                               int64_t O, int64_t R) {
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < O;
+         o += (int64_t)gridDim.x * blockDim.x) {
+        const T *xo = x + group_offset(go, 0, o);
+        T acc = Acc<T>::zero();
+        for (int64_t r = 0; r < R; ++r) acc = Acc<T>::add(acc, xo[group_offset(gr, 0, r)]);
+        y[group_offset(go, 1, o)] = acc;
+    }
+}
+
+// One warp per output (long reductions); the fastest reduced mode is walked
+// without division.
+template <typename T>
+__global__ void k_unary_warp(const T *__restrict__ x, T *__restrict__ y, ModeGroup go, ModeGroup gr,
+                             int64_t O, int64_t R) {
+    int lane = threadIdx.x % 32;
+    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
+    int64_t nwarps = (int64_t)gridDim.x * blockDim.x / 32;
+    int64_t e0 = gr.ext[0], s0 = gr.str[0][0];
+    ModeGroup rest = gr;
+    rest.n = gr.n - 1;
+    for (int i = 0; i < rest.n; ++i) {
+        rest.ext[i] = gr.ext[i + 1];
+        rest.str[0][i] = gr.str[0][i + 1];
+    }
+    int64_t outer = R / e0;
+    for (int64_t o = warp; o < O; o += nwarps) {
+        const T *xo = x + group_offset(go, 0, o);
+        T acc = Acc<T>::zero();
+        for (int64_t q = 0; q < outer; ++q) {
+            const T *xq = xo + group_offset(rest, 0, q);
+            for (int64_t r = lane; r < e0; r += 32) acc = Acc<T>::add(acc, xq[r * s0]);
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) acc = Acc<T>::add(acc, shfl_down(acc, d));
+        if (lane == 0) y[group_offset(go, 1, o)] = acc;
+    }
+}
+
+template <typename T>
+static int run_unary(const UnaryPlan &p, const T *x, T *y, cudaStream_t s) {
+    ModeGroup go = p.go, gr = p.gr;
+    if (go.n == 0) {
+        go.n = 1;
+        go.ext[0] = 1;
+        go.str[0][0] = go.str[1][0] = go.str[2][0] = 0;
+    }
+    if (gr.n == 0) {
+        gr.n = 1;
+        gr.ext[0] = 1;
+        gr.str[0][0] = gr.str[1][0] = gr.str[2][0] = 0;
+    }
+    if (p.R >= 64) {
+        int64_t blocks = std::min<int64_t>((p.O * 32 + 255) / 256, 152 * 16);
+        k_unary_warp<T><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(x, y, go, gr, p.O, p.R);
+    } else {
+        int64_t blocks = std::min<int64_t>((p.O + 255) / 256, 152 * 16);
+        k_unary_thread<T><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(x, y, go, gr, p.O, p.R);
+    }
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
+}
+
+int launch_unary(const UnaryPlan &p, const void *X, void *Y, cudaStream_t s) {
+    switch (p.x.dtype) {
+    case MGB_F32: return run_unary<float>(p, (const float *)X, (float *)Y, s);
+    case MGB_F64: return run_unary<double>(p, (const double *)X, (double *)Y, s);
+    case MGB_C32: return run_unary<float2>(p, (const float2 *)X, (float2 *)Y, s);
+    case MGB_C64: return run_unary<double2>(p, (const double2 *)X, (double2 *)Y, s);
+    }
+    return fail(MGB_ERR_ARGUMENT, "unary: bad dtype");
+}
+
+}  // namespace mgb

@@ -1,0 +1,302 @@
+"""binary_einsum / unary_einsum front-ends and the GB300 backend.
+
+Front-ends restate the label algebra of src/Operations/binary_einsum.jl:33-51
+and src/Operations/unary_einsum.jl:26-46; ``BackendGB300`` is the one backend
+this package adds, taken for (DomainCUDA, DomainCUDA) operands, and calls the
+C ABI of libmuscle_gb300.so (include/muscle_gb300.h). Label -> integer mode
+mapping follows ext/MuscleCUDAExt.jl:24-27 (first appearance in a, then b).
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from collections import OrderedDict
+
+import torch
+
+from . import _lib
+from ._lib import ArgumentError, check
+from .backend import Backend, DomainCUDA, choose_backend, register_rule
+from .tensor import Index, Tensor, empty_colmajor, intersect, nonunique, setdiff, union
+
+_DT = {torch.float32: _lib.F32, torch.float64: _lib.F64, torch.complex64: _lib.C32, torch.complex128: _lib.C64}
+_TORCH = {v: k for k, v in _DT.items()}
+
+
+def mgb_dtype(t: torch.dtype) -> int:
+    try:
+        return _DT[t]
+    except KeyError:
+        raise ArgumentError(f"element type {t} is not supported (Float32/64, ComplexF32/64)") from None
+
+
+def promote_eltype(a: torch.dtype, b: torch.dtype) -> torch.dtype:
+    return torch.promote_types(a, b)
+
+
+# ---------------------------------------------------------------------------
+# plans
+class Plan:
+    """Owns an mgb_plan handle."""
+
+    __slots__ = ("handle", "info", "__weakref__")
+
+    def __init__(self, handle):
+        self.handle = handle
+        info = _lib.PlanInfo()
+        check(_lib.load().mgb_plan_info_get(handle, ctypes.byref(info)))
+        self.info = info
+
+    @property
+    def workspace_bytes(self) -> int:
+        return int(self.info.workspace_bytes)
+
+    @property
+    def flops(self) -> float:
+        return float(self.info.flops)
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _lib.load().mgb_plan_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+class _PlanCache:
+    def __init__(self, capacity=4096):
+        self.cap = capacity
+        self.d: OrderedDict = OrderedDict()
+        self.lock = threading.Lock()
+
+    def get(self, key, make):
+        with self.lock:
+            p = self.d.get(key)
+            if p is not None:
+                self.d.move_to_end(key)
+                return p
+        p = make()
+        with self.lock:
+            self.d[key] = p
+            while len(self.d) > self.cap:
+                self.d.popitem(last=False)
+        return p
+
+
+_PLANS = _PlanCache()
+
+
+def _modes_for(*label_lists) -> dict:
+    m = {}
+    for labels in label_lists:
+        for i in labels:
+            if i not in m:
+                m[i] = len(m)
+    return m
+
+
+def _desc_args(t: torch.Tensor, labels, modes: dict):
+    return (mgb_dtype(t.dtype), tuple(modes[i] for i in labels), tuple(t.shape), tuple(t.stride()))
+
+
+def contraction_plan(a: torch.Tensor, ia, b: torch.Tensor, ib, c: torch.Tensor, ic, form: str = "auto",
+                     slices: int = 0) -> Plan:
+    modes = _modes_for(ia, ib, ic)
+    da, db, dc = _desc_args(a, ia, modes), _desc_args(b, ib, modes), _desc_args(c, ic, modes)
+    f = _lib.FORMS[form]
+    key = ("c", da, db, dc, f, int(slices))
+
+    def make():
+        lib = _lib.load()
+        (ad, ka), (bd, kb), (cd, kc) = (_lib.make_desc(*da), _lib.make_desc(*db), _lib.make_desc(*dc))
+        h = ctypes.c_void_p()
+        check(lib.mgb_contraction_plan(ctypes.byref(h), ctypes.byref(ad), ctypes.byref(bd), ctypes.byref(cd),
+                                       f, int(slices)), lib)
+        return Plan(h)
+
+    return _PLANS.get(key, make)
+
+
+def unary_plan(x: torch.Tensor, ix, y: torch.Tensor, iy) -> Plan:
+    modes = _modes_for(ix, iy)
+    dx, dy = _desc_args(x, ix, modes), _desc_args(y, iy, modes)
+    key = ("u", dx, dy)
+
+    def make():
+        lib = _lib.load()
+        (xd, kx), (yd, ky) = _lib.make_desc(*dx), _lib.make_desc(*dy)
+        h = ctypes.c_void_p()
+        check(lib.mgb_unary_plan(ctypes.byref(h), ctypes.byref(xd), ctypes.byref(yd)), lib)
+        return Plan(h)
+
+    return _PLANS.get(key, make)
+
+
+def _stream_handle(dev) -> int:
+    return torch.cuda.current_stream(dev).cuda_stream
+
+
+def _require_cuda(*ts):
+    for t in ts:
+        if not t.is_cuda:
+            raise ArgumentError("BackendGB300 needs device-resident (CUDA) arrays")
+
+
+def _workspace(nbytes: int, dev):
+    if nbytes == 0:
+        return None, 0
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    return ws, ws.data_ptr()
+
+
+def contract_into(c: torch.Tensor, ic, a: torch.Tensor, ia, b: torch.Tensor, ib, form="auto", slices=0,
+                  workspace: torch.Tensor | None = None) -> torch.Tensor:
+    """C[ic] = sum A[ia] * B[ib] on the current stream (cuTENSOR semantics)."""
+    _require_cuda(a, b, c)
+    plan = contraction_plan(a, ia, b, ib, c, ic, form, slices)
+    need = plan.workspace_bytes
+    if workspace is not None and workspace.numel() >= need:
+        ws, wp = workspace, workspace.data_ptr()
+    else:
+        ws, wp = _workspace(need, c.device)
+    lib = _lib.load()
+    check(lib.mgb_contract(plan.handle, a.data_ptr(), b.data_ptr(), c.data_ptr(), wp, need,
+                           _stream_handle(c.device)), lib)
+    return c
+
+
+# ---------------------------------------------------------------------------
+class BackendGB300(Backend):
+    """The GB300 backend. ``form`` is one of "auto" (Ozaki for Float64 /
+    ComplexF64 results, BF16x3 for Float32 / ComplexF32), "plain" (native
+    FP64 DMMA / FP32 FFMA), "ozaki" or "bf16x3"; ``slices`` is the Ozaki
+    slice count (3..8, 0 = default 7)."""
+
+    def __init__(self, form: str = "auto", slices: int = 0):
+        if form not in _lib.FORMS:
+            raise ArgumentError(f"unknown form {form!r}")
+        self.form = form
+        self.slices = int(slices)
+
+    # binary_einsum(::BackendGB300, inds_c, a, b)  (called at binary_einsum.jl:50)
+    def binary_einsum(self, inds_c, a: Tensor, b: Tensor) -> Tensor:
+        inds_c = [i if isinstance(i, Index) else Index(i) for i in inds_c]
+        sizes = {}
+        for t in (a, b):
+            for d, i in enumerate(t.inds):
+                sizes.setdefault(i, t.data.shape[d])
+        for i in inds_c:
+            if i not in sizes:
+                raise ArgumentError(f"output index {i} is in neither operand")
+        dt = promote_eltype(a.dtype, b.dtype)
+        c = empty_colmajor([sizes[i] for i in inds_c], dt, a.data.device)
+        C = Tensor(c, inds_c)
+        self.binary_einsum_(C, a, b)
+        return C
+
+    # binary_einsum!(::BackendGB300, c, a, b)  (called at binary_einsum.jl:68)
+    def binary_einsum_(self, c: Tensor, a: Tensor, b: Tensor) -> Tensor:
+        contract_into(c.data, c.inds, a.data, a.inds, b.data, b.inds, self.form, self.slices)
+        return c
+
+    # unary_einsum(::BackendGB300, inds_y, x)  (called at unary_einsum.jl:35)
+    def unary_einsum(self, inds_y, x: Tensor) -> Tensor:
+        inds_y = [i if isinstance(i, Index) else Index(i) for i in inds_y]
+        for i in inds_y:
+            if i not in x.inds:
+                raise ArgumentError("Output indices must be a subset of input indices")
+        y = empty_colmajor([x.size(i) for i in inds_y], x.dtype, x.data.device)
+        Y = Tensor(y, inds_y)
+        self.unary_einsum_(Y, x)
+        return Y
+
+    # unary_einsum!(::BackendGB300, y, x)  (called at unary_einsum.jl:44)
+    def unary_einsum_(self, y: Tensor, x: Tensor) -> Tensor:
+        _require_cuda(x.data, y.data)
+        if x.dtype != y.dtype:
+            raise ArgumentError("unary_einsum!: X and Y must share the element type")
+        plan = unary_plan(x.data, x.inds, y.data, y.inds)
+        lib = _lib.load()
+        check(lib.mgb_unary(plan.handle, x.data.data_ptr(), y.data.data_ptr(), None, 0,
+                            _stream_handle(y.data.device)), lib)
+        return y
+
+
+for _f, _doms in (("binary_einsum", (DomainCUDA, DomainCUDA)), ("binary_einsum_", (DomainCUDA, DomainCUDA, DomainCUDA)),
+                  ("unary_einsum", (DomainCUDA,)), ("unary_einsum_", (DomainCUDA, DomainCUDA))):
+    register_rule(_f, _doms, BackendGB300)
+
+
+# ---------------------------------------------------------------------------
+# front-ends
+def binary_einsum(a: Tensor, b: Tensor, dims=None, out=None) -> Tensor:
+    """Contract ``a`` and ``b`` (src/Operations/binary_einsum.jl:33-51).
+
+    dims: labels to contract (default: the shared labels);
+    out:  output labels (default: a's free labels, then b's, in order)."""
+    ia, ib = a.inds, b.inds
+    if dims is None:
+        dims = intersect(ia, ib)
+    elif isinstance(dims, Index):
+        dims = [dims]
+    inds_sum = intersect(dims, ia, ib)
+    inds_c = list(out) if out is not None else setdiff(union(ia, ib), inds_sum)
+    backend = choose_backend(binary_einsum, a.data, b.data)
+    return backend.binary_einsum(inds_c, a, b)
+
+
+def binary_einsum_(c: Tensor, a: Tensor, b: Tensor) -> Tensor:
+    """In-place contraction into ``c`` (src/Operations/binary_einsum.jl:57-70)."""
+    backend = choose_backend(binary_einsum_, c.data, a.data, b.data)
+    backend.binary_einsum_(c, a, b)
+    return c
+
+
+def unary_einsum(x: Tensor, dims=None, out=None) -> Tensor:
+    """Trace / diagonal / partial sum (src/Operations/unary_einsum.jl:26-36).
+
+    dims: labels summed over (default: the repeated labels);
+    out:  output labels (default: the remaining unique labels)."""
+    if dims is None:
+        dims = nonunique(x.inds)
+    elif isinstance(dims, Index):
+        dims = [dims]
+    inds_sum = intersect(dims, x.inds)
+    inds_y = list(out) if out is not None else setdiff(x.inds, inds_sum)
+    backend = choose_backend(unary_einsum, x.data)
+    return backend.unary_einsum(inds_y, x)
+
+
+def unary_einsum_(y: Tensor, x: Tensor) -> Tensor:
+    """In-place unary contraction into ``y`` (src/Operations/unary_einsum.jl:42-46)."""
+    backend = choose_backend(unary_einsum_, y.data, x.data)
+    backend.unary_einsum_(y, x)
+    return y
+
+
+def permutedims(t: Tensor, perm) -> Tensor:
+    """Device permutation by labels (src/Tensor.jl:316-319) through the
+    permutation kernel; ``perm`` is a list of Index labels or positions."""
+    if t.ndim == 0:
+        return t
+    labels = [t.inds[p] if isinstance(p, int) else (p if isinstance(p, Index) else Index(p)) for p in perm]
+    if sorted(map(repr, labels)) != sorted(map(repr, t.inds)):
+        raise ArgumentError("permutation must use every label once")
+    _require_cuda(t.data)
+    y = empty_colmajor([t.size(i) for i in labels], t.dtype, t.data.device)
+    modes = _modes_for(t.inds)
+    (xd, kx) = _lib.make_desc(*_desc_args(t.data, t.inds, modes))
+    (yd, ky) = _lib.make_desc(*_desc_args(y, labels, modes))
+    lib = _lib.load()
+    check(lib.mgb_permute(ctypes.byref(xd), ctypes.byref(yd), t.data.data_ptr(), y.data_ptr(),
+                          _stream_handle(y.device)), lib)
+    return Tensor(y, labels)
+
+
+def device_status(device=None) -> int:
+    """Reads and clears the device status word (0 = no timeout recorded)."""
+    lib = _lib.load()
+    st = ctypes.c_int32(0)
+    check(lib.mgb_device_status(_stream_handle(device or torch.cuda.current_device()), ctypes.byref(st)), lib)
+    return int(st.value)

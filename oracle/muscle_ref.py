@@ -1,0 +1,307 @@
+"""CPU oracle for Muscle.jl's tensor contractions — TEST INFRASTRUCTURE ONLY.
+
+This module restates, in numpy, the algorithm of Muscle.jl's host backend so
+that the GPU library can be checked against it. It is imported only by
+``tests/``, ``__graft_entry__.smoke()`` (as the checker) and ``bench.py``'s
+CPU-baseline / reference arm; the product (``muscle.jl_gb300``) never calls it.
+
+Followed reference code (paths inside the Muscle.jl repository, v0.3.20):
+  * label algebra of the front-end ......... src/Operations/binary_einsum.jl:33-51
+  * BackendBase: permute -> GEMM -> permute . src/Operations/binary_einsum.jl:76-96
+  * in-place variant (inds(c) == [left; right]) src/Operations/binary_einsum.jl:98-121
+  * permutedims by labels .................. src/Tensor.jl:316-319
+  * findperm (label order comparison) ...... src/Index.jl:20-34
+  * batch (hyper) labels kept in the output  test/integration/cuda.jl:126-145,170-180
+                                             (cuTENSOR semantics, ext/MuscleCUDAExt.jl:10-41)
+  * unary trace / diagonal / sums .......... src/Operations/unary_einsum.jl:26-46,
+                                             test/integration/omeinsum.jl:6-100
+The GEMM is numpy's matmul, i.e. OpenBLAS (scipy-openblas), the same BLAS
+family Julia's LinearAlgebra uses. Julia arrays are column-major: reshapes
+here use order="F" so that the folded matrices are the same as Julia's.
+
+Parity status: the reference is Julia and no Julia exists in this build
+environment, so this restatement cannot be run side by side with it. It is
+pinned against every known-answer assertion of the reference's own tests for
+this path (tests/golden/kat_cases.json, generated by tests/golden/make_kat.py);
+bit-level parity with Julia's BLAS is unpinned (and not expected: BLAS
+summation order is unspecified). Floating-point parity is asserted at the
+spec tolerances (1e-13 / 1e-5 relative Frobenius).
+"""
+from __future__ import annotations
+
+from fractions import Fraction
+
+import numpy as np
+
+
+class ArgumentError(ValueError):
+    pass
+
+
+class DimensionMismatch(ValueError):
+    pass
+
+
+# ---------------------------------------------------------------- label algebra
+def _unique(xs):
+    out = []
+    for x in xs:
+        if x not in out:
+            out.append(x)
+    return out
+
+
+def setdiff(xs, ys):
+    ys = list(ys)
+    return [x for x in _unique(xs) if x not in ys]
+
+
+def intersect(*seqs):
+    first, rest = seqs[0], [list(s) for s in seqs[1:]]
+    return [x for x in _unique(first) if all(x in r for r in rest)]
+
+
+def union(*seqs):
+    out = []
+    for s in seqs:
+        for x in s:
+            if x not in out:
+                out.append(x)
+    return out
+
+
+def nonunique(xs):
+    seen, rep = [], []
+    for x in xs:
+        if x in seen:
+            if x not in rep:
+                rep.append(x)
+        else:
+            seen.append(x)
+    return rep
+
+
+def front_inds_c(ia, ib, dims=None, out=None):
+    """Output labels chosen by binary_einsum(a, b; dims, out)
+    (src/Operations/binary_einsum.jl:33-40)."""
+    if dims is None:
+        dims = intersect(ia, ib)
+    inds_sum = intersect(dims, ia, ib)
+    return list(out) if out is not None else setdiff(union(ia, ib), inds_sum)
+
+
+def front_inds_y(ix, dims=None, out=None):
+    """Output labels chosen by unary_einsum(x; dims, out)
+    (src/Operations/unary_einsum.jl:26-32)."""
+    if dims is None:
+        dims = nonunique(ix)
+    inds_sum = intersect(dims, ix)
+    return list(out) if out is not None else setdiff(ix, inds_sum)
+
+
+# ---------------------------------------------------------------- contractions
+def _permute(x, labels, to):
+    """permutedims by labels (src/Tensor.jl:316-319)."""
+    return np.transpose(x, [labels.index(i) for i in to]) if to else x
+
+
+def _prod(xs):
+    p = 1
+    for x in xs:
+        p *= int(x)
+    return p
+
+
+def backend_base(inds_c, a, ia, b, ib):
+    """BackendBase binary_einsum (src/Operations/binary_einsum.jl:76-96)."""
+    ia, ib, inds_c = list(ia), list(ib), list(inds_c)
+    inds_contract = intersect(ia, ib)
+    inds_left = setdiff(ia, inds_contract)
+    inds_right = setdiff(ib, inds_contract)
+    if any(i in inds_contract for i in inds_c) or sorted(map(repr, inds_c)) != sorted(
+        map(repr, setdiff(union(ia, ib), inds_contract))
+    ):
+        raise ArgumentError("`BackendBase` can't deal with hyperindices. Load OMEinsum and use `BackendOMEinsum` instead.")
+    sl = [a.shape[ia.index(i)] for i in inds_left]
+    sr = [b.shape[ib.index(i)] for i in inds_right]
+    sk = [a.shape[ia.index(i)] for i in inds_contract]
+    a_mat = _permute(a, ia, inds_left + inds_contract).reshape(_prod(sl), _prod(sk), order="F")
+    b_mat = _permute(b, ib, inds_contract + inds_right).reshape(_prod(sk), _prod(sr), order="F")
+    c_mat = a_mat @ b_mat
+    c = c_mat.reshape(sl + sr, order="F")
+    return _permute(c, inds_left + inds_right, inds_c)
+
+
+def contract(a, ia, b, ib, ic):
+    """Contraction with cuTENSOR label semantics, as expected of the CUDA path
+    by test/integration/cuda.jl:126-145,170-180: labels of A and B absent from C
+    are summed; labels in A, B and C are batch labels. Computed as BackendBase
+    (permute -> BLAS GEMM -> permute) once per batch entry."""
+    ia, ib, ic = list(ia), list(ib), list(ic)
+    for x, lx in ((a, ia), (b, ib)):
+        if len(set(map(repr, lx))) != len(lx):
+            raise ArgumentError("repeated label in a binary contraction operand")
+    size = {}
+    for x, lx in ((a, ia), (b, ib)):
+        for d, i in enumerate(lx):
+            if i in size and size[i] != x.shape[d]:
+                raise DimensionMismatch(f"label {i} has different extents")
+            size[i] = x.shape[d]
+    for i in ic:
+        if i not in size:
+            raise ArgumentError(f"output label {i} is in neither operand")
+    batch = [i for i in ia if i in ib and i in ic]
+    contr = [i for i in ia if i in ib and i not in ic]
+    left = [i for i in ia if i not in ib]
+    right = [i for i in ib if i not in ia]
+    for i in left + right:
+        if i not in ic:
+            raise ArgumentError(f"label {i} appears in one operand only and not in the output")
+    dt = np.result_type(a.dtype, b.dtype)
+    M, N, K, L = (_prod(size[i] for i in g) for g in (left, right, contr, batch))
+    am = _permute(a, ia, left + contr + batch).astype(dt, copy=False).reshape(M, K, L, order="F")
+    bm = _permute(b, ib, contr + right + batch).astype(dt, copy=False).reshape(K, N, L, order="F")
+    cm = np.empty((M, N, L), dtype=dt, order="F")
+    for l in range(L):
+        cm[:, :, l] = am[:, :, l] @ bm[:, :, l]
+    c = cm.reshape([size[i] for i in left + right + batch], order="F")
+    return _permute(c, left + right + batch, ic)
+
+
+def unary(x, ix, iy):
+    """unary_einsum with OMEinsum semantics (ext/MuscleOMEinsumExt.jl:25-38):
+    repeated labels of X take the diagonal, labels absent from Y are summed."""
+    ix, iy = list(ix), list(iy)
+    for i in iy:
+        if i not in ix:
+            raise ArgumentError("Output indices must be a subset of input indices")
+    labels = _unique(ix)
+    letters = {lab: chr(ord("a") + n) for n, lab in enumerate(labels)}
+    spec = "".join(letters[i] for i in ix) + "->" + "".join(letters[i] for i in iy)
+    return np.einsum(spec, x)
+
+
+def exact_entries(a, ia, b, ib, ic, positions):
+    """Exact (rational) values of selected output entries, used to bound the
+    oracle's own rounding error. positions: list of index tuples of C."""
+    ia, ib, ic = list(ia), list(ib), list(ic)
+    contr = [i for i in ia if i in ib and i not in ic]
+    size = {i: a.shape[d] for d, i in enumerate(ia)}
+    size.update({i: b.shape[d] for d, i in enumerate(ib)})
+    out = []
+    cx = np.iscomplexobj(a) or np.iscomplexobj(b)
+    for pos in positions:
+        fixed = dict(zip(ic, pos))
+        re, im = Fraction(0), Fraction(0)
+        for kidx in np.ndindex(*[size[i] for i in contr]):
+            lab = dict(fixed)
+            lab.update(zip(contr, kidx))
+            av = a[tuple(lab[i] for i in ia)]
+            bv = b[tuple(lab[i] for i in ib)]
+            ar, ai = Fraction(float(np.real(av))), Fraction(float(np.imag(av)))
+            br, bi = Fraction(float(np.real(bv))), Fraction(float(np.imag(bv)))
+            re += ar * br - ai * bi
+            im += ar * bi + ai * br
+        out.append(complex(float(re), float(im)) if cx else float(re))
+    return out
+
+
+def rel_fro(x, ref):
+    """Relative Frobenius error ||x - ref|| / ||ref||."""
+    x = np.asarray(x)
+    ref = np.asarray(ref)
+    den = np.linalg.norm(ref.ravel())
+    num = np.linalg.norm((x - ref).ravel())
+    return float(num / den) if den else float(num)
+
+
+# ---------------------------------------------------------------- generators
+def _cnormal(rng, shape, dtype, scale=1.0):
+    if np.issubdtype(dtype, np.complexfloating):
+        re = rng.standard_normal(shape)
+        im = rng.standard_normal(shape)
+        return (scale * (re + 1j * im)).astype(dtype)
+    return (scale * rng.standard_normal(shape)).astype(dtype)
+
+
+def colmajor(x):
+    return np.asfortranarray(x)
+
+
+def gen_config1(seed=0, dtype=np.complex128, dim=32):
+    """Plain C64: A(i,j,k,l), B(k,m,l,n), all extents ``dim`` (32 in the
+    benchmark), re/im iid N(0,1), PCG64(seed)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = colmajor(_cnormal(rng, (dim,) * 4, dtype))
+    b = colmajor(_cnormal(rng, (dim,) * 4, dtype))
+    return (a, ["i", "j", "k", "l"]), (b, ["k", "m", "l", "n"]), ["i", "j", "m", "n"]
+
+
+def gen_config2a(seed=0, dtype=np.complex128, scale=1):
+    """A(a,b,c,d,e) = 64x96x64x48x32, B(e,c,f,a) = 32x64x128x64 -> (b,d,f);
+    ``scale`` divides every extent (for CPU-sized parity cases)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ea = [64 // scale, 96 // scale, 64 // scale, 48 // scale, 32 // scale]
+    eb = [32 // scale, 64 // scale, 128 // scale, 64 // scale]
+    a = colmajor(_cnormal(rng, ea, dtype))
+    b = colmajor(_cnormal(rng, eb, dtype))
+    return (a, ["a", "b", "c", "d", "e"]), (b, ["e", "c", "f", "a"]), ["b", "d", "f"]
+
+
+def gen_config2b(seed=0, dtype=np.complex128, scale=1):
+    """MPS bond: A(l,p,r) = 512x4x512, B(r,q,s) = 512x4x512 -> (l,p,q,s)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = colmajor(_cnormal(rng, (512 // scale, 4, 512 // scale), dtype))
+    b = colmajor(_cnormal(rng, (512 // scale, 4, 512 // scale), dtype))
+    return (a, ["l", "p", "r"]), (b, ["r", "q", "s"]), ["l", "p", "q", "s"]
+
+
+def loguniform_complex(rng, shape, dtype=np.complex128, lo=-20.0, hi=20.0):
+    """|z| = 2^U(lo,hi), arg z = U(0, 2 pi) (real dtypes: random sign)."""
+    mag = np.exp2(rng.uniform(lo, hi, size=shape))
+    if np.issubdtype(dtype, np.complexfloating):
+        ph = rng.uniform(0.0, 2 * np.pi, size=shape)
+        return (mag * np.exp(1j * ph)).astype(dtype)
+    sgn = np.where(rng.uniform(size=shape) < 0.5, -1.0, 1.0)
+    return (mag * sgn).astype(dtype)
+
+
+def gen_config3(seed=0, dtype=np.complex128, n=8192, k1=128, k2=64):
+    """Precision form: A(i,k1,k2) = n x k1 x k2, B(k2,j,k1) = k2 x n x k1
+    (M = N = n, K = k1 k2), log-uniform magnitudes over 2^-20..2^20."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = colmajor(loguniform_complex(rng, (n, k1, k2), dtype))
+    b = colmajor(loguniform_complex(rng, (k2, n, k1), dtype))
+    return (a, ["i", "k1", "k2"]), (b, ["k2", "j", "k1"]), ["i", "j"]
+
+
+PEPS_CHI = (8, 12, 16, 24, 32, 48, 64)
+PEPS_CAP = 1 << 24  # elements of A + B + C per instance
+
+
+def peps_instance(seed, dtype=np.complex128, cap=PEPS_CAP, max_tries=1000):
+    """One batching-form instance: a rank-5 site (physical dim 2, four bonds of
+    one bond dimension chi drawn from PEPS_CHI) contracted with a neighbour
+    over 1-3 shared bonds; entries iid complex N(0, 1/chi). Instances whose
+    A + B + C exceed ``cap`` elements are redrawn from the same stream.
+    Returns ((a, ia), (b, ib), ic, tries)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    for tries in range(1, max_tries + 1):
+        chi = int(rng.choice(PEPS_CHI))
+        nsh = int(rng.integers(1, 4))
+        bonds = ["u", "r", "d", "l"]
+        shared = list(rng.choice(bonds, size=nsh, replace=False))
+        ia = ["p"] + bonds
+        ib = ["q"] + shared + [f"x{t}" for t in range(4 - nsh)]
+        ea = [2] + [chi] * 4
+        eb = [2] + [chi] * 4
+        ic = ["p"] + [b for b in bonds if b not in shared] + ["q"] + [f"x{t}" for t in range(4 - nsh)]
+        na, nb = 2 * chi**4, 2 * chi**4
+        nc = 4 * chi ** (2 * (4 - nsh))
+        if na + nb + nc > cap:
+            continue
+        sc = 1.0 / np.sqrt(2.0 * chi)  # complex N(0, 1/chi): re, im ~ N(0, 1/(2 chi))
+        a = colmajor(_cnormal(rng, ea, dtype, sc))
+        b = colmajor(_cnormal(rng, eb, dtype, sc))
+        return (a, ia), (b, ib), ic, tries
+    raise RuntimeError("no instance under the cap")

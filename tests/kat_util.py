@@ -1,0 +1,33 @@
+"""Helpers that turn kat_cases.json entries into arrays and expected values."""
+import numpy as np
+
+NP = {"float32": np.float32, "float64": np.float64, "complex64": np.complex64, "complex128": np.complex128}
+
+
+def fill_value(f):
+    return complex(f[0], f[1]) if isinstance(f, list) else f
+
+
+def make_array(spec):
+    dt = NP[spec["dtype"]]
+    if spec.get("iota"):
+        n = int(np.prod(spec["shape"]))
+        return np.asfortranarray(np.arange(1, n + 1, dtype=dt).reshape(spec["shape"], order="F"))
+    return np.asfortranarray(np.full(spec["shape"], fill_value(spec["fill"]), dtype=dt))
+
+
+def expected_binary(case, exp, a, b):
+    """Expected array of a binary case (fill or the test's own formula)."""
+    if "fill" in exp:
+        return np.full(exp["shape"], fill_value(exp["fill"]))
+    if exp["formula"].startswith("reshape"):
+        a_mat = a.reshape(2, 12, order="F")
+        b_mat = np.transpose(b, (2, 0, 1)).reshape(12, 5, order="F")
+        return a_mat @ b_mat
+    c = np.zeros((2, 4, 5), dtype=np.result_type(a, b))
+    for i in range(2):
+        for j in range(3):
+            for k in range(4):
+                for l in range(5):
+                    c[i, k, l] += a[i, j, k] * b[k, l, j]
+    return c

@@ -1,0 +1,156 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports
+every declared symbol, plan construction (label algebra, errors, workspace
+sizes), and the Python mirror of Muscle.jl's data model and dispatch."""
+import ctypes
+import os
+import re
+
+import pytest
+import torch
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", f)).read()
+            names |= set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(mgb_\w+)\s*\(", src, re.M))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    import muscle_gb300
+    from muscle_gb300 import _lib
+
+    lib = muscle_gb300.library()
+    names = declared_symbols()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _lib.SIGNATURES, n
+    assert lib.mgb_version().startswith(b"muscle_gb300")
+
+
+def _plan(a, b, c, form=0, slices=0):
+    from muscle_gb300 import _lib
+
+    lib = _lib.load()
+    da, ka = _lib.make_desc(*a)
+    db, kb = _lib.make_desc(*b)
+    dc, kc = _lib.make_desc(*c)
+    h = ctypes.c_void_p()
+    st = lib.mgb_contraction_plan(ctypes.byref(h), ctypes.byref(da), ctypes.byref(db), ctypes.byref(dc), form, slices)
+    info = _lib.PlanInfo()
+    if st == 0:
+        assert lib.mgb_plan_info_get(h, ctypes.byref(info)) == 0
+        lib.mgb_plan_destroy(h)
+    return st, info, lib.mgb_last_error().decode()
+
+
+def colmajor(shape):
+    s, out = 1, []
+    for e in shape:
+        out.append(s)
+        s *= e
+    return out
+
+
+def desc(dtype, modes, shape):
+    return (dtype, modes, shape, colmajor(shape))
+
+
+def test_plan_config1_folds_to_gemm():
+    from muscle_gb300 import _lib
+
+    st, info, _ = _plan(desc(_lib.C64, [0, 1, 2, 3], [32] * 4), desc(_lib.C64, [2, 4, 3, 5], [32] * 4),
+                        desc(_lib.C64, [0, 1, 4, 5], [32] * 4), _lib.FORM_OZAKI, 7)
+    assert st == 0
+    assert (info.m, info.n, info.k, info.batch) == (1024, 1024, 1024, 1)
+    assert info.flops == 8.0 * 1024**3
+    assert info.slices == 7 and info.form == _lib.FORM_OZAKI
+    # A and B slices (7 x M x 2K and 7 x 2N x 2K bf16) + scales
+    assert info.workspace_bytes >= 7 * 1024 * 2048 * 2 + 7 * 2048 * 2048 * 2
+
+
+def test_plan_errors_map_to_julia_exceptions():
+    from muscle_gb300 import _lib
+
+    # extent mismatch of a shared label -> DimensionMismatch
+    st, _, msg = _plan(desc(_lib.F64, [0, 1], [2, 3]), desc(_lib.F64, [1, 2], [4, 5]), desc(_lib.F64, [0, 2], [2, 5]))
+    assert st == _lib.ERR_DIMENSION_MISMATCH and "extent" in msg
+    # output label absent from the operands -> ArgumentError
+    st, _, _ = _plan(desc(_lib.F64, [0, 1], [2, 3]), desc(_lib.F64, [1, 2], [3, 5]), desc(_lib.F64, [0, 7], [2, 5]))
+    assert st == _lib.ERR_ARGUMENT
+    # wrong result element type -> ArgumentError
+    st, _, _ = _plan(desc(_lib.F64, [0, 1], [2, 3]), desc(_lib.C64, [1, 2], [3, 5]), desc(_lib.F64, [0, 2], [2, 5]))
+    assert st == _lib.ERR_ARGUMENT
+    # a free label dropped from the output -> ArgumentError
+    st, _, _ = _plan(desc(_lib.F64, [0, 1], [2, 3]), desc(_lib.F64, [1, 2], [3, 5]), desc(_lib.F64, [0], [2]))
+    assert st == _lib.ERR_ARGUMENT
+    # Ozaki on a Float32 result -> unsupported
+    st, _, _ = _plan(desc(_lib.F32, [0, 1], [2, 3]), desc(_lib.F32, [1, 2], [3, 5]), desc(_lib.F32, [0, 2], [2, 5]),
+                     _lib.FORM_OZAKI)
+    assert st == _lib.ERR_UNSUPPORTED
+    # slice count out of range
+    st, _, _ = _plan(desc(_lib.F64, [0, 1], [2, 3]), desc(_lib.F64, [1, 2], [3, 5]), desc(_lib.F64, [0, 2], [2, 5]),
+                     _lib.FORM_OZAKI, 12)
+    assert st == _lib.ERR_ARGUMENT
+
+
+def test_plan_batch_and_scalar():
+    from muscle_gb300 import _lib
+
+    st, info, _ = _plan(desc(_lib.F64, [0, 1, 9], [2, 3, 6]), desc(_lib.F64, [1, 2, 9], [3, 4, 6]),
+                        desc(_lib.F64, [9, 0, 2], [6, 2, 4]), _lib.FORM_PLAIN)
+    assert st == 0 and (info.m, info.n, info.k, info.batch) == (2, 4, 3, 6)
+    st, info, _ = _plan(desc(_lib.F64, [], []), desc(_lib.F64, [0, 1], [2, 3]), desc(_lib.F64, [1, 0], [3, 2]),
+                        _lib.FORM_PLAIN)
+    assert st == 0 and (info.m, info.n, info.k) == (1, 6, 1)
+
+
+def test_plan_folds_config2a_groups():
+    from muscle_gb300 import _lib
+
+    # A(a,b,c,d,e) B(e,c,f,a) -> C(b,d,f): M = b*d, N = f, K = a*c*e
+    st, info, _ = _plan(desc(_lib.C64, [0, 1, 2, 3, 4], [64, 96, 64, 48, 32]), desc(_lib.C64, [4, 2, 5, 0], [32, 64, 128, 64]),
+                        desc(_lib.C64, [1, 3, 5], [96, 48, 128]), _lib.FORM_PLAIN)
+    assert st == 0 and (info.m, info.n, info.k) == (96 * 48, 128, 64 * 64 * 32)
+    assert abs(info.flops - 6.18e11) / 6.18e11 < 0.01
+
+
+def test_data_model_and_dispatch():
+    import muscle_gb300 as m
+
+    i, j = m.Index("i"), m.Index("j")
+    assert m.Index(i) == i and hash(m.Index("i")) == hash(i)
+    with pytest.raises(m.ArgumentError):
+        m.Tensor(torch.ones(2, 3), [i])
+    with pytest.raises(m.DimensionMismatch):
+        m.Tensor(torch.ones(2, 3), [i, i])
+    t = m.Tensor(torch.ones(2, 3, 2), [i, j, i])
+    assert m.nonunique(t.inds) == [i]
+    assert t.size(j) == 3
+    # host arrays have no rule in this package (they belong to Muscle's BackendBase)
+    with pytest.raises(m.ArgumentError):
+        m.binary_einsum(m.Tensor(torch.ones(2, 3), ["i", "j"]), m.Tensor(torch.ones(3), ["j"]))
+    with pytest.raises(m.ArgumentError):
+        m.unary_einsum(t)
+    # scoped override wins over the rule table and is restored afterwards
+    with m.with_backend(m.BackendGB300("plain")) as be:
+        assert m.choose_backend(m.binary_einsum, t.data, t.data) == be
+    assert m.with_backend(lambda: m.choose_backend(m.unary_einsum, t.data), m.BackendGB300("ozaki", 6)) == m.BackendGB300("ozaki", 6)
+    with pytest.raises(m.ArgumentError):
+        m.choose_backend(m.binary_einsum, t.data, t.data)
+    # a backend that lacks the method raises like the reference's fallback methods
+    with pytest.raises(m.ArgumentError):
+        m.BackendBase().binary_einsum([], t, t)
+
+
+def test_column_major_allocation():
+    import muscle_gb300 as m
+
+    x = m.empty_colmajor([2, 3, 4], torch.float64, "cpu")
+    assert x.shape == (2, 3, 4) and x.stride() == (1, 2, 6)
+    assert m.empty_colmajor([], torch.float64, "cpu").dim() == 0

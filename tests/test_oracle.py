@@ -1,0 +1,91 @@
+"""The oracle against the known answers of Muscle.jl's own tests (CPU only)."""
+import numpy as np
+import pytest
+
+from oracle import muscle_ref as ref
+from tests.kat_util import expected_binary, make_array
+
+
+def test_kat_binary_base_and_gpu_semantics(kat_cases):
+    n = 0
+    for case in kat_cases:
+        if case["kind"] != "binary":
+            continue
+        a, b = make_array(case["a"]), make_array(case["b"])
+        ia, ib = case["a"]["inds"], case["b"]["inds"]
+        ic = ref.front_inds_c(ia, ib, case["dims"], case["out"])
+        eb = case["expect_base"]
+        if "raises" in eb:
+            with pytest.raises(ref.ArgumentError):
+                ref.backend_base(ic, a, ia, b, ib)
+        else:
+            c = ref.backend_base(ic, a, ia, b, ib)
+            assert list(ic) == eb["inds"], case["name"]
+            assert list(np.shape(c)) == eb["shape"], case["name"]
+            want = expected_binary(case, eb, a, b)
+            if "fill" in eb:
+                assert np.array_equal(c, want), case["name"]
+            else:
+                assert np.allclose(c, want, rtol=1e-12), case["name"]
+        eg = case["expect_gpu"]
+        c = ref.contract(a, ia, b, ib, ic)
+        assert list(ic) == eg["inds"], case["name"]
+        assert list(np.shape(c)) == eg["shape"], case["name"]
+        want = expected_binary(case, eg, a, b)
+        if "fill" in eg:
+            assert np.array_equal(c, want), case["name"]
+        else:
+            assert np.allclose(c, want, rtol=1e-12), case["name"]
+        n += 1
+    assert n >= 30
+
+
+def test_kat_unary(kat_cases):
+    for case in kat_cases:
+        if case["kind"] != "unary":
+            continue
+        x = make_array(case["x"])
+        ix = case["x"]["inds"]
+        iy = case["inplace"] if case["inplace"] is not None else ref.front_inds_y(ix, case["dims"], case["out"])
+        y = ref.unary(x, ix, iy)
+        assert list(iy) == case["expect"]["inds"], case["name"]
+        assert np.array_equal(y, np.full(case["expect"]["shape"], case["expect"]["fill"])), case["name"]
+
+
+def test_kat_permute(kat_cases):
+    case = [c for c in kat_cases if c["kind"] == "permute"][0]
+    x = make_array(case["x"])
+    y = ref._permute(x, case["x"]["inds"], case["perm"])
+    assert list(y.shape) == case["expect"]["shape"]
+    assert np.array_equal(y, np.transpose(x, (2, 0, 1)))
+
+
+def test_contract_matches_exact_rational():
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((3, 4, 5)) + 1j * rng.standard_normal((3, 4, 5))
+    b = rng.standard_normal((5, 2, 4)) + 1j * rng.standard_normal((5, 2, 4))
+    c = ref.contract(a, ["i", "k", "l"], b, ["l", "j", "k"], ["j", "i"])
+    pos = [(0, 0), (1, 2), (0, 1)]
+    ex = ref.exact_entries(a, ["i", "k", "l"], b, ["l", "j", "k"], ["j", "i"], pos)
+    for p, e in zip(pos, ex):
+        assert abs(c[p] - e) <= 1e-14 * max(1.0, abs(e))
+
+
+def test_front_end_defaults():
+    assert ref.front_inds_c(["i", "j"], ["j", "k"]) == ["i", "k"]
+    assert ref.front_inds_c(["i", "j", "b"], ["j", "k", "b"], dims=["j"]) == ["i", "b", "k"]
+    assert ref.front_inds_y(["i", "j", "i"]) == ["j"]
+    assert ref.nonunique(["i", "j", "i", "j", "i"]) == ["i", "j"]
+
+
+def test_generators_are_seeded():
+    (a1, _), (b1, _), _ = ref.gen_config1(seed=0, dim=4)
+    (a2, _), (b2, _), _ = ref.gen_config1(seed=0, dim=4)
+    assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
+    (a, ia), (b, ib), ic = ref.gen_config3(seed=0, n=64, k1=8, k2=4)
+    mags = np.log2(np.abs(a))
+    assert mags.min() >= -20 and mags.max() <= 20
+    for s in range(20):
+        (pa, pia), (pb, pib), pic, tries = ref.peps_instance(100 + s)
+        n = pa.size + pb.size + int(np.prod([dict(zip(pia + pib, pa.shape + pb.shape))[i] for i in pic]))
+        assert n <= ref.PEPS_CAP
