@@ -230,18 +230,36 @@ for _f, _doms in (("binary_einsum", (DomainCUDA, DomainCUDA)), ("binary_einsum_"
 
 # ---------------------------------------------------------------------------
 # front-ends
+def _labels(xs) -> list:
+    if isinstance(xs, (Index, str)):
+        xs = [xs]
+    return [x if isinstance(x, Index) else Index(x) for x in xs]
+
+
+def binary_inds_c(ia, ib, dims=None, out=None) -> list:
+    """Output labels of binary_einsum(a, b; dims, out)
+    (src/Operations/binary_einsum.jl:33-40)."""
+    if out is not None:
+        return _labels(out)
+    dims = intersect(ia, ib) if dims is None else _labels(dims)
+    inds_sum = intersect(dims, ia, ib)
+    return setdiff(union(ia, ib), inds_sum)
+
+
+def unary_inds_y(ix, dims=None, out=None) -> list:
+    """Output labels of unary_einsum(x; dims, out) (src/Operations/unary_einsum.jl:26-32)."""
+    if out is not None:
+        return _labels(out)
+    dims = nonunique(ix) if dims is None else _labels(dims)
+    return setdiff(ix, intersect(dims, ix))
+
+
 def binary_einsum(a: Tensor, b: Tensor, dims=None, out=None) -> Tensor:
     """Contract ``a`` and ``b`` (src/Operations/binary_einsum.jl:33-51).
 
     dims: labels to contract (default: the shared labels);
     out:  output labels (default: a's free labels, then b's, in order)."""
-    ia, ib = a.inds, b.inds
-    if dims is None:
-        dims = intersect(ia, ib)
-    elif isinstance(dims, Index):
-        dims = [dims]
-    inds_sum = intersect(dims, ia, ib)
-    inds_c = list(out) if out is not None else setdiff(union(ia, ib), inds_sum)
+    inds_c = binary_inds_c(a.inds, b.inds, dims, out)
     backend = choose_backend(binary_einsum, a.data, b.data)
     return backend.binary_einsum(inds_c, a, b)
 
@@ -258,12 +276,7 @@ def unary_einsum(x: Tensor, dims=None, out=None) -> Tensor:
 
     dims: labels summed over (default: the repeated labels);
     out:  output labels (default: the remaining unique labels)."""
-    if dims is None:
-        dims = nonunique(x.inds)
-    elif isinstance(dims, Index):
-        dims = [dims]
-    inds_sum = intersect(dims, x.inds)
-    inds_y = list(out) if out is not None else setdiff(x.inds, inds_sum)
+    inds_y = unary_inds_y(x.inds, dims, out)
     backend = choose_backend(unary_einsum, x.data)
     return backend.unary_einsum(inds_y, x)
 

@@ -225,7 +225,7 @@ def _cnormal(rng, shape, dtype, scale=1.0):
 
 
 def colmajor(x):
-    return np.asfortranarray(x)
+    return np.array(x, order="F")  # keeps 0-d arrays 0-d
 
 
 def gen_config1(seed=0, dtype=np.complex128, dim=32):

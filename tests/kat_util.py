@@ -12,8 +12,8 @@ def make_array(spec):
     dt = NP[spec["dtype"]]
     if spec.get("iota"):
         n = int(np.prod(spec["shape"]))
-        return np.asfortranarray(np.arange(1, n + 1, dtype=dt).reshape(spec["shape"], order="F"))
-    return np.asfortranarray(np.full(spec["shape"], fill_value(spec["fill"]), dtype=dt))
+        return np.array(np.arange(1, n + 1, dtype=dt).reshape(spec["shape"], order="F"), order="F")
+    return np.array(np.full(spec["shape"], fill_value(spec["fill"]), dtype=dt), order="F")
 
 
 def expected_binary(case, exp, a, b):

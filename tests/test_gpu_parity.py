@@ -19,7 +19,7 @@ def rand(rng, shape, dtype):
     x = rng.standard_normal(shape)
     if np.issubdtype(dtype, np.complexfloating):
         x = x + 1j * rng.standard_normal(shape)
-    return np.asfortranarray(x.astype(dtype))
+    return np.array(x.astype(dtype), order="F")
 
 
 CASES = [
@@ -145,6 +145,7 @@ def test_ozaki_exact_on_integer_data():
     assert np.abs(want).max() < 2.0**52
     got, _ = run(np.asfortranarray(a), ["i", "j"], np.asfortranarray(b), ["j", "k"], ["i", "k"], "ozaki", 7)
     assert np.array_equal(got, want)
+    a, b = a[:, :2048], b[:2048]  # complex sums stay below 2^52 too
     ac, bc = (a + 1j * a[::-1]).copy(order="F"), (b - 1j * b[:, ::-1]).copy(order="F")
     wantc = ac @ bc
     gotc, _ = run(ac, ["i", "j"], bc, ["j", "k"], ["i", "k"], "ozaki", 7)
@@ -160,7 +161,7 @@ def test_ozaki_slice_sweep_and_loguniform_spread():
     for s in range(3, 9):
         got, _ = run(a, ia, b, ib, ic, "ozaki", s)
         errs[s] = ref.rel_fro(got, want)
-    assert all(errs[s + 1] < errs[s] for s in range(3, 8) if errs[s] > 1e-15), errs
+    assert all(errs[s + 1] < errs[s] for s in range(3, 7)), errs
     assert errs[7] <= F64_TOL and errs[8] <= F64_TOL, errs
     got, _ = run(a, ia, b, ib, ic, "plain")
     assert ref.rel_fro(got, want) <= F64_TOL

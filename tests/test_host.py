@@ -154,3 +154,25 @@ def test_column_major_allocation():
     x = m.empty_colmajor([2, 3, 4], torch.float64, "cpu")
     assert x.shape == (2, 3, 4) and x.stride() == (1, 2, 6)
     assert m.empty_colmajor([], torch.float64, "cpu").dim() == 0
+
+
+def test_front_end_label_algebra_matches_oracle(kat_cases):
+    """The product's label algebra equals the oracle's on every KAT case,
+    with labels given as plain tags or as Index objects."""
+    import muscle_gb300 as m
+    from muscle_gb300.ops import binary_inds_c, unary_inds_y
+    from oracle import muscle_ref as ref
+
+    for case in kat_cases:
+        if case["kind"] == "binary":
+            ia = [m.Index(x) for x in case["a"]["inds"]]
+            ib = [m.Index(x) for x in case["b"]["inds"]]
+            want = ref.front_inds_c(case["a"]["inds"], case["b"]["inds"], case["dims"], case["out"])
+            for wrap in (lambda v: v, lambda v: None if v is None else [m.Index(x) for x in v]):
+                got = binary_inds_c(ia, ib, wrap(case["dims"]), wrap(case["out"]))
+                assert [i.tag for i in got] == want, case["name"]
+                assert [i.tag for i in got] == case["expect_gpu"]["inds"], case["name"]
+        elif case["kind"] == "unary" and case["inplace"] is None:
+            ix = [m.Index(x) for x in case["x"]["inds"]]
+            got = unary_inds_y(ix, case["dims"], case["out"])
+            assert [i.tag for i in got] == case["expect"]["inds"], case["name"]
