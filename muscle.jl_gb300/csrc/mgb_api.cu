@@ -366,9 +366,10 @@ static int contract_impl(mgb_plan plan, const void *A, const void *B, void *C, v
         if (plan->timing) MGB_CUDA_CHECK(cudaEventRecord(plan->ev[1], s));
         return MGB_OK;
     }
-    if (!A || !B || !C) return fail(MGB_ERR_ARGUMENT, "null operand pointer");
+    if (!C) return fail(MGB_ERR_ARGUMENT, "null output pointer");
     if (plan->timing) MGB_CUDA_CHECK(cudaEventRecord(plan->ev[1], s));
-    if (cp.K == 0) return launch_fill_zero(C, nc, cp.c.dtype, cp.c, s);
+    if (cp.K == 0) return launch_fill_zero(C, nc, cp.c.dtype, cp.c, s);  // empty sum
+    if (!A || !B) return fail(MGB_ERR_ARGUMENT, "null operand pointer");
     if (cp.form == MGB_FORM_PLAIN) {
         ContractionPlan q = cp;
         const void *a = A, *b = B;

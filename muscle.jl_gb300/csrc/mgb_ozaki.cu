@@ -20,8 +20,12 @@
 //   d <= 15, so the readout is exact for every S <= 8 supported here.
 //
 // BF16X3 (Float32 / ComplexF32 results)
-//   x = hi + mid + lo, three bf16 pieces; the six products with
-//   piece-index sum <= 4 accumulate in one float32 TMEM accumulator.
+//   x = hi + mid + lo, three bf16 pieces (exact for normal floats); the six
+//   products with piece-index sum <= 4 are kept. The tensor core accumulates
+//   in float32 with truncation, whose bias grows with the number of
+//   accumulations, so hi*hi and the five smaller products go to two separate
+//   TMEM accumulators, double-buffered, read out every KC = 256 k and summed
+//   in registers with Kahan compensation.
 //
 // Complex operands are embedded as real GEMMs: A_e[m][2k+p] = part_p(A[m,k]),
 // B_e[2n+q][2k+p] holds [[Br, -Bi], [Bi, Br]] so that C_e[m][2n+q] is part q
@@ -53,6 +57,7 @@ constexpr int OZ_BM = 128;     // rows of A per CTA (TMEM lanes)
 constexpr int OZ_BN = 64;      // embedded rows of B per CTA
 constexpr int OZ_BK = 32;      // k per stage (64-byte swizzled rows)
 constexpr int OZ_EPI_WARPS = 8;
+constexpr int OZ_GROUP_M = 16;  // row tiles per rasterisation band
 constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;
 constexpr int OZ_A_TILE = OZ_BM * OZ_BK * 2;  // 8192 bytes per slice
 constexpr int OZ_B_TILE = OZ_BN * OZ_BK * 2;  // 4096 bytes per slice
@@ -63,8 +68,8 @@ __host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (OZ_A_TILE 
 __host__ __device__ constexpr int oz_stages(int S) {
     return (OZ_SMEM_BUDGET / oz_stage_bytes(S)) < 4 ? (OZ_SMEM_BUDGET / oz_stage_bytes(S)) : 4;
 }
-__host__ __device__ constexpr int oz_tmem_cols(int ng) {
-    return ng * OZ_BN <= 64 ? 64 : ng * OZ_BN <= 128 ? 128 : ng * OZ_BN <= 256 ? 256 : 512;
+__host__ __device__ constexpr int oz_tmem_cols(int nacc) {
+    return nacc * OZ_BN <= 64 ? 64 : nacc * OZ_BN <= 128 ? 128 : nacc * OZ_BN <= 256 ? 256 : 512;
 }
 __host__ __device__ constexpr int oz_smem_bytes(int S) {
     return oz_stages(S) * oz_stage_bytes(S) + 1024 /*align*/ + 512 /*barriers*/;
@@ -97,18 +102,21 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: false when the CTA aborted or this wait timed out.
+// Bounded wait: false when the CTA aborted or this wait timed out (about a
+// second of clock64 cycles, checked every 256 tries).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag,
                                           int32_t *status) {
     if (mbar_try(bar, parity)) return true;
     long long t0 = clock64();
-    while (true) {
+    for (uint32_t n = 1;; ++n) {
         if (mbar_try(bar, parity)) return true;
-        if (*abort_flag) return false;
-        if (clock64() - t0 > OZ_TIMEOUT_CYCLES) {
-            *abort_flag = 1;
-            atomicCAS(status, 0, (int32_t)MGB_ERR_DEVICE_TIMEOUT);
-            return false;
+        if ((n & 255) == 0) {
+            if (*abort_flag) return false;
+            if (clock64() - t0 > OZ_TIMEOUT_CYCLES) {
+                *abort_flag = 1;
+                atomicCAS(status, 0, (int32_t)MGB_ERR_DEVICE_TIMEOUT);
+                return false;
+            }
         }
     }
 }
@@ -145,6 +153,20 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
+// Predicated MMA: issued only when `issue` != 0. Keeping the issuing thread's
+// instruction stream free of branches matters: a taken branch between two
+// tcgen05.mma instructions costs far more issue time than extra arithmetic.
+__device__ __forceinline__ void tc_mma_if(uint32_t issue, uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "setp.ne.b32 q, %5, 0;\n\t"
+        "@q tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate), "r"(issue)
+        : "memory");
+}
+
 __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
@@ -175,6 +197,10 @@ __device__ __forceinline__ double x96_to_double(uint32_t w0, uint32_t w1, uint32
     return fma(__ll2double_rn(hi), 4294967296.0, __uint2double_rn(w0));
 }
 
+// Staggered exact chunks: digit group g closes a chunk after k block kb when
+// g == (kb + 1) % kcb, and every group closes its last chunk after the last
+// block. Each chunk spans at most kcb blocks (KC = kcb * 32 embedded k), so
+// the float32 partial sums stay exact; one group is read out per k block.
 // K-major operand tile, 64-byte swizzle: rows of 64 B, 8-row atoms of 512 B.
 __device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
     uint64_t d = 0;
@@ -452,26 +478,48 @@ template <int S, bool EXACT, bool CX>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_oz_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const OzGemmArgs args) {
-    constexpr int NG = EXACT ? S : 1;
+    // NG accumulators (digit groups, or hi/lo for BF16X3) per buffer; BF16X3
+    // double-buffers them so the MMA never waits for the readout.
+    constexpr int NG = EXACT ? S : 2;
+    constexpr int NB = EXACT ? 1 : 2;
+    // ROT: one spare accumulator slot; a digit group whose chunk ends moves to
+    // the free slot and leaves the old one to the epilogue (S <= 7 fits TMEM).
+    constexpr bool ROT = EXACT && S <= 7;
+    constexpr int NSLOT = ROT ? S + 1 : NG * NB;
     constexpr int NST = oz_stages(S);
     constexpr int STAGE = oz_stage_bytes(S);
-    constexpr int TCOLS = oz_tmem_cols(NG);
+    constexpr int TCOLS = oz_tmem_cols(NSLOT);
     static_assert(NST >= 2, "need at least two pipeline stages");
-    static_assert(NG * OZ_BN <= 512, "TMEM holds at most 512 columns");
+    static_assert(NSLOT * OZ_BN <= 512, "TMEM holds at most 512 columns");
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + NST * STAGE);
     uint64_t *full = bars;              // [NST]
     uint64_t *empty = bars + NST;       // [NST]
-    uint64_t *acc_full = bars + 2 * NST;
-    uint64_t *acc_empty = bars + 2 * NST + 1;  // [NG]
-    uint64_t *done = bars + 2 * NST + 1 + NG;
+    constexpr int NFULL = EXACT ? NG : NB;      // chunk-complete barriers
+    uint64_t *acc_full = bars + 2 * NST;        // [NFULL]
+    uint64_t *acc_empty = acc_full + NFULL;     // [NSLOT] (per physical accumulator)
+    uint64_t *done = acc_empty + NSLOT;
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    const int64_t n0 = (int64_t)blockIdx.x * OZ_BN, m0 = (int64_t)blockIdx.y * OZ_BM;
+    // Grouped rasterisation: consecutive CTAs walk a band of OZ_GROUP_M row
+    // tiles across all column tiles, so the slices of A and B they read are
+    // shared in L2 by the CTAs resident at the same time.
+    int64_t m_tile, n_tile;
+    {
+        const int64_t nm = gridDim.y, nn = gridDim.x;
+        const int64_t t = (int64_t)blockIdx.y * nn + blockIdx.x;
+        const int64_t band = t / (OZ_GROUP_M * nn);
+        const int64_t first = band * OZ_GROUP_M;
+        const int64_t rows = min((int64_t)OZ_GROUP_M, nm - first);
+        const int64_t r = t - band * OZ_GROUP_M * nn;
+        m_tile = first + r % rows;
+        n_tile = r / rows;
+    }
+    const int64_t n0 = n_tile * OZ_BN, m0 = m_tile * OZ_BM;
     const int l = blockIdx.z;
 
     if (tid == 0) {
@@ -479,8 +527,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             mbar_init(smem_u32(full + s), 1);
             mbar_init(smem_u32(empty + s), 1);
         }
-        mbar_init(smem_u32(acc_full), 1);
-        for (int g = 0; g < NG; ++g) mbar_init(smem_u32(acc_empty + g), OZ_EPI_WARPS);
+        for (int b = 0; b < NFULL; ++b) mbar_init(smem_u32(acc_full + b), 1);
+        for (int g = 0; g < NSLOT; ++g) mbar_init(smem_u32(acc_empty + g), OZ_EPI_WARPS);
         mbar_init(smem_u32(done), 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -523,49 +571,152 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             const uint32_t idesc = oz_idesc();
-            int chunk = 0;
-            uint32_t touched = 0;
             bool ok = true;
-            for (int kb = 0; kb < nkb && ok; ++kb) {
-                int s = kb % NST;
-                uint32_t round = kb / NST;
-                bool chunk_start = (kb % kcb) == 0;
-                if (!mbar_wait(smem_u32(full + s), round & 1, abort_flag, args.status)) {
-                    ok = false;
-                    break;
-                }
-                tc_fence_after();
-                const uint32_t a_base = smem_u32(smem + s * STAGE);
-                const uint32_t b_base = a_base + S * OZ_A_TILE;
+            if constexpr (ROT) {
+                // slot of group g: 4 bits of `map`; `freeslot` holds the spare one
+                uint32_t map = 0, freeslot = S, fill = 0;  // fill bit x: parity of chunks left in slot x
 #pragma unroll
-                for (int k16 = 0; k16 < OZ_BK / 16; ++k16) {
+                for (int g = 0; g < S; ++g) map |= (uint32_t)g << (4 * g);
+                for (int kb = 0; kb < nkb && ok; ++kb) {
+                    const int s = kb % NST;
+                    const uint32_t round = kb / NST;
+                    if (!mbar_wait(smem_u32(full + s), round & 1, abort_flag, args.status)) {
+                        ok = false;
+                        break;
+                    }
+                    const int gs = kb == 0 ? -1 : kb % kcb;  // group starting a new chunk
+                    if (gs >= 0 && gs < S) {
+                        const uint32_t nw = freeslot;
+                        freeslot = (map >> (4 * gs)) & 15u;
+                        map = (map & ~(15u << (4 * gs))) | (nw << (4 * gs));
+                        // the chunk previously left in slot nw must have been read out
+                        ok = mbar_wait(smem_u32(acc_empty + nw), ((fill >> nw) & 1u) ^ 1u, abort_flag, args.status);
+                        if (!ok) break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_base = smem_u32(smem + s * STAGE);
+                    const uint64_t ad0 = sw64_desc(a_base);
+                    const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
 #pragma unroll
-                    for (int i = 0; i < S; ++i) {
+                    for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
 #pragma unroll
-                        for (int j = 0; j < S - i; ++j) {
-                            const int g = EXACT ? i + j : 0;
-                            const bool first = chunk_start && k16 == 0 && !(touched & (1u << g));
-                            if (first && ok) {
-                                // group g of the previous chunk must have been read out
-                                ok = mbar_wait(smem_u32(acc_empty + g), (chunk & 1) ^ 1, abort_flag,
-                                               args.status);
-                                tc_fence_after();
-                                touched |= 1u << g;
+                        for (int i = 0; i < S; ++i)
+#pragma unroll
+                            for (int j = 0; j < S - i; ++j) {
+                                const int g = i + j;
+                                const uint32_t d = tmem + ((map >> (4 * g)) & 15u) * OZ_BN;
+                                const uint32_t acc = (k16 == 0 && i == 0 && (kb == 0 || g == gs)) ? 0u : 1u;
+                                tc_mma_if(1u, d, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
+                                          bd0 + (uint64_t)((j * OZ_B_TILE + k16 * 32) >> 4), idesc, acc);
                             }
-                            if (ok) {
-                                uint64_t ad = sw64_desc(a_base + i * OZ_A_TILE + k16 * 32);
-                                uint64_t bd = sw64_desc(b_base + j * OZ_B_TILE + k16 * 32);
-                                tc_mma(tmem + g * OZ_BN, ad, bd, idesc, first ? 0u : 1u);
-                            }
-                        }
+                    tc_commit(smem_u32(empty + s));
+                    if (kb == nkb - 1) {
+                        for (int g = 0; g < NG; ++g) tc_commit(smem_u32(acc_full + g));
+                    } else if ((kb + 1) % kcb < S) {
+                        const int ge = (kb + 1) % kcb;  // group whose chunk ends here
+                        tc_commit(smem_u32(acc_full + ge));
+                        fill ^= 1u << ((map >> (4 * ge)) & 15u);
                     }
                 }
-                if (!ok) break;
-                tc_commit(smem_u32(empty + s));
-                if ((kb % kcb) == kcb - 1 || kb == nkb - 1) {
-                    tc_commit(smem_u32(acc_full));
-                    ++chunk;
-                    touched = 0;
+            } else if constexpr (EXACT) {
+                // Group g closes its chunks at k blocks kb with (kb + 1 - g) % kcb == 0
+                // (staggered), so one group is read out per k block; the group that
+                // starts a chunk gets its MMAs last, after the other groups' work.
+                uint32_t par = 0;  // bit g: parity of group g's completed chunks
+                for (int kb = 0; kb < nkb && ok; ++kb) {
+                    const int s = kb % NST;
+                    const uint32_t round = kb / NST;
+                    if (!mbar_wait(smem_u32(full + s), round & 1, abort_flag, args.status)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_base = smem_u32(smem + s * STAGE);
+                    const uint64_t ad0 = sw64_desc(a_base);
+                    const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
+                    // group starting a chunk in this k block (-1: block 0, where all start)
+                    const int gs = kb == 0 ? -1 : kb % kcb;
+                    const uint32_t not_first = kb == 0 ? 0u : 1u;
+                    // pass 1: every group except gs, i-major so that consecutive MMAs
+                    // go to different accumulators; fully unrolled and predicated
+#pragma unroll
+                    for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
+#pragma unroll
+                        for (int i = 0; i < S; ++i)
+#pragma unroll
+                            for (int j = 0; j < S - i; ++j) {
+                                const int g = i + j;
+                                const uint32_t acc = (k16 == 0 && i == 0) ? not_first : 1u;
+                                tc_mma_if(g != gs, tmem + g * OZ_BN, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
+                                          bd0 + (uint64_t)((j * OZ_B_TILE + k16 * 32) >> 4), idesc, acc);
+                            }
+                    // pass 2: group gs, once the epilogue has read its previous chunk
+                    if (gs >= 0 && gs < NG) {
+                        ok = mbar_wait(smem_u32(acc_empty + gs), ((par >> gs) & 1) ^ 1, abort_flag, args.status);
+                        if (!ok) break;
+                        tc_fence_after();
+                        const uint32_t dg = tmem + gs * OZ_BN;
+#pragma unroll
+                        for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
+#pragma unroll
+                            for (int i = 0; i < S; ++i) {
+                                const int j = gs - i;  // >= 0 exactly when i <= gs
+                                tc_mma_if(i <= gs, dg, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
+                                          bd0 + (uint64_t)((max(j, 0) * OZ_B_TILE + k16 * 32) >> 4), idesc,
+                                          (k16 == 0 && i == 0) ? 0u : 1u);
+                            }
+                    }
+                    tc_commit(smem_u32(empty + s));
+                    if (kb == nkb - 1) {
+                        for (int g = 0; g < NG; ++g) tc_commit(smem_u32(acc_full + g));
+                    } else if ((kb + 1) % kcb < NG) {
+                        const int g = (kb + 1) % kcb;
+                        tc_commit(smem_u32(acc_full + g));
+                        par ^= 1u << g;
+                    }
+                }
+            } else {
+                int chunk = 0;
+                for (int kb = 0; kb < nkb && ok; ++kb) {
+                    const int s = kb % NST;
+                    const uint32_t round = kb / NST;
+                    const bool chunk_start = (kb % kcb) == 0;
+                    const int buf = chunk % NB;       // accumulator buffer of this chunk
+                    const uint32_t use = chunk / NB;  // earlier uses of that buffer
+                    if (!mbar_wait(smem_u32(full + s), round & 1, abort_flag, args.status)) {
+                        ok = false;
+                        break;
+                    }
+                    if (chunk_start) {
+                        // both accumulators of this buffer must have been read out
+                        ok = mbar_wait(smem_u32(acc_empty + buf * NG + 0), (use & 1) ^ 1, abort_flag, args.status) &&
+                             mbar_wait(smem_u32(acc_empty + buf * NG + 1), (use & 1) ^ 1, abort_flag, args.status);
+                        if (!ok) break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_base = smem_u32(smem + s * STAGE);
+                    const uint64_t ad0 = sw64_desc(a_base);
+                    const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
+                    const uint32_t t_hi = tmem + (buf * NG + 0) * OZ_BN, t_lo = tmem + (buf * NG + 1) * OZ_BN;
+                    const uint32_t not_first = chunk_start ? 0u : 1u;
+#pragma unroll
+                    for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
+#pragma unroll
+                        for (int i = 0; i < S; ++i)
+#pragma unroll
+                            for (int j = 0; j < S - i; ++j) {
+                                // hi*hi apart from the five smaller products
+                                const bool hi = (i | j) == 0;
+                                const bool lo_first = i == 0 && j == 1;  // first product into t_lo
+                                const uint32_t acc = (k16 == 0 && (hi || lo_first)) ? not_first : 1u;
+                                tc_mma_if(1u, hi ? t_hi : t_lo, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
+                                          bd0 + (uint64_t)((j * OZ_B_TILE + k16 * 32) >> 4), idesc, acc);
+                            }
+                    tc_commit(smem_u32(empty + s));
+                    if ((kb % kcb) == kcb - 1 || kb == nkb - 1) {
+                        tc_commit(smem_u32(acc_full + buf));
+                        ++chunk;
+                    }
                 }
             }
             // wait for every MMA this thread issued before TMEM is released
@@ -581,7 +732,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         // EXACT: one 96-bit two's-complement integer per output column,
         // X = sum_d G_d 2^(W (S + 1 - d)), held in w0 (bits 0-31), w1, w2.
         uint32_t w0[EXACT ? 32 : 1], w1[EXACT ? 32 : 1], w2[EXACT ? 32 : 1];
-        float accf[EXACT ? 1 : 32];
+        // BF16X3: Kahan-compensated float32 sum over the chunks
+        float accf[EXACT ? 1 : 32], comp[EXACT ? 1 : 32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             if (EXACT) {
@@ -590,41 +742,115 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 w2[j] = 0;
             } else {
                 accf[j] = 0.f;
+                comp[j] = 0.f;
             }
         }
         bool ok = true;
-        for (int c = 0; c < nchunks && ok; ++c) {
-            if (!mbar_wait(smem_u32(acc_full), c & 1, abort_flag, args.status)) {
-                ok = false;
-                break;
-            }
-            tc_fence_after();
+        if constexpr (ROT) {
+            // Same events as below; the slot of each group follows the MMA side's map.
+            uint32_t map = 0, freeslot = S, par = 0;
+#pragma unroll
+            for (int g = 0; g < S; ++g) map |= (uint32_t)g << (4 * g);
+            const int nev = nkb - 1 + NG;
 #pragma unroll 1
-            for (int g = 0; g < NG; ++g) {
+            for (int e = 0; e < nev; ++e) {
+                const int g = e < nkb - 1 ? (e + 1) % kcb : e - (nkb - 1);
+                if (g >= NG) continue;
+                const uint32_t x = (map >> (4 * g)) & 15u;
+                if (!mbar_wait(smem_u32(acc_full + g), (par >> g) & 1, abort_flag, args.status)) {
+                    ok = false;
+                    break;
+                }
+                par ^= 1u << g;
+                tc_fence_after();
+                uint32_t v[32];
+                tc_ld32(tbase + x * OZ_BN, v);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(acc_empty + x));
+                if (e < nkb - 1) {  // group g continues in the free slot
+                    const uint32_t nw = freeslot;
+                    freeslot = x;
+                    map = (map & ~(15u << (4 * g))) | (nw << (4 * g));
+                }
+                const int sh = OZ_W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
+                if (sh < 32) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
+                        add96(w0[j], w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32),
+                              t < 0 ? 0xFFFFFFFFu : 0u);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
+                        add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
+                    }
+                }
+            }
+        } else if constexpr (EXACT) {
+            // Readout events in order: after k block kb < nkb - 1 group
+            // (kb + 1) % kcb (when it exists) closes a chunk; after the last
+            // block every group closes its last chunk.
+            uint32_t par = 0;  // bit g: parity of group g's chunks read so far
+            const int nev = nkb - 1 + NG;
+#pragma unroll 1
+            for (int e = 0; e < nev; ++e) {
+                const int g = e < nkb - 1 ? (e + 1) % kcb : e - (nkb - 1);
+                if (g >= NG) continue;
+                if (!mbar_wait(smem_u32(acc_full + g), (par >> g) & 1, abort_flag, args.status)) {
+                    ok = false;
+                    break;
+                }
+                par ^= 1u << g;
+                tc_fence_after();
                 uint32_t v[32];
                 tc_ld32(tbase + g * OZ_BN, v);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(acc_empty + g));
-                if (EXACT) {
-                    const int sh = OZ_W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
-                    if (sh < 32) {
+                const int sh = OZ_W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
+                if (sh < 32) {
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
-                            add96(w0[j], w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32),
-                                  t < 0 ? 0xFFFFFFFFu : 0u);
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
-                            add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
-                        }
+                    for (int j = 0; j < 32; ++j) {
+                        int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
+                        add96(w0[j], w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32),
+                              t < 0 ? 0xFFFFFFFFu : 0u);
                     }
                 } else {
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) accf[j] += __uint_as_float(v[j]);
+                    for (int j = 0; j < 32; ++j) {
+                        int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
+                        add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
+                    }
+                }
+            }
+        } else {
+            for (int c = 0; c < nchunks && ok; ++c) {
+                const int buf = c % NB;
+                if (!mbar_wait(smem_u32(acc_full + buf), (c / NB) & 1, abort_flag, args.status)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                // hi*hi and the smaller products of this chunk, then one compensated add
+                uint32_t vh[32], vl[32];
+                tc_ld32(tbase + (buf * NG + 0) * OZ_BN, vh);
+                tc_ld32(tbase + (buf * NG + 1) * OZ_BN, vl);
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_arrive(smem_u32(acc_empty + buf * NG + 0));
+                    mbar_arrive(smem_u32(acc_empty + buf * NG + 1));
+                }
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    float x = __uint_as_float(vh[j]) + __uint_as_float(vl[j]);
+                    float y = x - comp[j];
+                    float t = accf[j] + y;
+                    comp[j] = (t - accf[j]) - y;
+                    accf[j] = t;
                 }
             }
         }
@@ -860,7 +1086,7 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
     a.Ne = p.n_e;
     a.N = p.N;
     a.nkb = (int32_t)((p.k_e + OZ_BK - 1) / OZ_BK);
-    a.kcb = exact ? OZ_KC / OZ_BK : a.nkb;
+    a.kcb = OZ_KC / OZ_BK;
     a.S = S;
     a.expA = ea;
     a.expB = eb;

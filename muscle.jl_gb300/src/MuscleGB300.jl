@@ -1,0 +1,166 @@
+"""
+    MuscleGB300
+
+A Muscle.jl backend for device-resident tensors on NVIDIA GB300 (sm_103a).
+Loading this package registers `BackendGB300` as the backend for
+`binary_einsum`, `binary_einsum!`, `unary_einsum` and `unary_einsum!` on
+`(DomainCUDA, ...)` operands (the rule tables of
+src/Operations/binary_einsum.jl:20-31 and src/Operations/unary_einsum.jl:20-24),
+and implements those operations by `ccall` into `libmuscle_gb300.so`
+(C ABI in include/muscle_gb300.h). `with_backend(f, BackendGB300(...))`
+selects a form explicitly.
+"""
+module MuscleGB300
+
+using CUDA
+using Muscle
+using Muscle: Backend, DomainCUDA, Index, Tensor, inds
+
+export BackendGB300
+
+const libmgb = get(ENV, "MUSCLE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libmuscle_gb300.so"))
+
+const FORMS = Dict(:auto => Cint(0), :plain => Cint(1), :ozaki => Cint(2), :bf16x3 => Cint(3))
+
+"""
+    BackendGB300(; form=:auto, slices=0)
+
+`form`: `:auto` (Ozaki emulation for Float64/ComplexF64 results, BF16x3 for
+Float32/ComplexF32), `:plain` (native FP64 DMMA / FP32 FFMA), `:ozaki`,
+`:bf16x3`. `slices`: Ozaki slice count (3..8; 0 means 7).
+"""
+struct BackendGB300 <: Backend
+    form::Cint
+    slices::Cint
+end
+BackendGB300(; form::Symbol=:auto, slices::Integer=0) = BackendGB300(FORMS[form], Cint(slices))
+
+# mirrors `mgb_tensor_desc`
+struct TensorDesc
+    dtype::Cint
+    rank::Cint
+    modes::Ptr{Cint}
+    extents::Ptr{Int64}
+    strides::Ptr{Int64}
+end
+
+dtype_code(::Type{Float32}) = Cint(0)
+dtype_code(::Type{Float64}) = Cint(1)
+dtype_code(::Type{ComplexF32}) = Cint(2)
+dtype_code(::Type{ComplexF64}) = Cint(3)
+dtype_code(::Type{T}) where {T} = throw(ArgumentError("eltype $T is not supported by BackendGB300"))
+
+function check(status::Cint)
+    status == 0 && return nothing
+    msg = unsafe_string(ccall((:mgb_last_error, libmgb), Cstring, ()))
+    status == 1 && throw(ArgumentError(msg))
+    status == 2 && throw(DimensionMismatch(msg))
+    status == 3 && throw(ArgumentError(msg))
+    status == 7 && throw(CUDA.OutOfGPUMemoryError(0))
+    error("libmuscle_gb300 status $status: $msg")
+end
+
+# labels -> integer modes by first appearance (ext/MuscleCUDAExt.jl:24-27)
+function modemap(tensors...)
+    m = Dict{Index,Cint}()
+    for t in tensors, i in inds(t)
+        haskey(m, i) || (m[i] = Cint(length(m)))
+    end
+    m
+end
+
+# arrays kept alive by the caller with GC.@preserve
+descarrays(t::Tensor, m) = (Cint[m[i] for i in inds(t)], Int64[size(t)...], Int64[strides(parent(t))...])
+function desc(t::Tensor, arrs)
+    modes, ext, str = arrs
+    TensorDesc(dtype_code(eltype(t)), Cint(ndims(t)), pointer(modes), pointer(ext), pointer(str))
+end
+
+function with_plan(f, create)
+    plan = Ref{Ptr{Cvoid}}(C_NULL)
+    check(create(plan))
+    try
+        f(plan[])
+    finally
+        ccall((:mgb_plan_destroy, libmgb), Cint, (Ptr{Cvoid},), plan[])
+    end
+end
+
+function workspace(plan)
+    bytes = Ref{UInt64}(0)
+    check(ccall((:mgb_plan_workspace_size, libmgb), Cint, (Ptr{Cvoid}, Ref{UInt64}), plan, bytes))
+    bytes[] == 0 ? (CU_NULL, UInt64(0)) : (CuArray{UInt8}(undef, bytes[]), bytes[])
+end
+
+# binary_einsum(::Backend, inds_c, a, b)  (src/Operations/binary_einsum.jl:50)
+function Muscle.binary_einsum(be::BackendGB300, inds_c, a::Tensor, b::Tensor)
+    sizes = Dict{Index,Int}()
+    for t in (a, b), (i, s) in zip(inds(t), size(t))
+        sizes[i] = s
+    end
+    T = Base.promote_eltype(a, b)
+    c = Tensor(similar(parent(a), T, Tuple(sizes[i] for i in inds_c)), collect(inds_c))
+    return Muscle.binary_einsum!(be, c, a, b)
+end
+
+# binary_einsum!(::Backend, c, a, b)  (src/Operations/binary_einsum.jl:68)
+function Muscle.binary_einsum!(be::BackendGB300, c::Tensor, a::Tensor, b::Tensor)
+    m = modemap(a, b, c)
+    aa, ab, ac = descarrays(a, m), descarrays(b, m), descarrays(c, m)
+    GC.@preserve aa ab ac begin
+        da, db, dc = Ref(desc(a, aa)), Ref(desc(b, ab)), Ref(desc(c, ac))
+        with_plan(p -> ccall((:mgb_contraction_plan, libmgb), Cint,
+                             (Ptr{Ptr{Cvoid}}, Ref{TensorDesc}, Ref{TensorDesc}, Ref{TensorDesc}, Cint, Cint),
+                             p, da, db, dc, be.form, be.slices)) do plan
+            ws, nbytes = workspace(plan)
+            check(ccall((:mgb_contract, libmgb), Cint,
+                        (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, UInt64, CUDA.CUstream),
+                        plan, parent(a), parent(b), parent(c), ws, nbytes, CUDA.stream()))
+        end
+    end
+    return c
+end
+
+# unary_einsum(::Backend, inds_y, x)  (src/Operations/unary_einsum.jl:35)
+function Muscle.unary_einsum(be::BackendGB300, inds_y, x::Tensor)
+    y = Tensor(similar(parent(x), Tuple(size(x, i) for i in inds_y)), collect(inds_y))
+    return Muscle.unary_einsum!(be, y, x)
+end
+
+# unary_einsum!(::Backend, y, x)  (src/Operations/unary_einsum.jl:44)
+function Muscle.unary_einsum!(::BackendGB300, y::Tensor, x::Tensor)
+    m = modemap(x, y)
+    ax, ay = descarrays(x, m), descarrays(y, m)
+    GC.@preserve ax ay begin
+        dx, dy = Ref(desc(x, ax)), Ref(desc(y, ay))
+        with_plan(p -> ccall((:mgb_unary_plan, libmgb), Cint,
+                             (Ptr{Ptr{Cvoid}}, Ref{TensorDesc}, Ref{TensorDesc}), p, dx, dy)) do plan
+            check(ccall((:mgb_unary, libmgb), Cint,
+                        (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, UInt64, CUDA.CUstream),
+                        plan, parent(x), parent(y), CU_NULL, UInt64(0), CUDA.stream()))
+        end
+    end
+    return y
+end
+
+"""
+    MuscleGB300.enable!()
+
+Make `BackendGB300` the rule for device-resident operands, replacing the
+`BackendCuTENSOR` / `BackendOMEinsum` rules of
+src/Operations/binary_einsum.jl:21,30 and src/Operations/unary_einsum.jl:21,24.
+Muscle defines those methods itself, so they are replaced at run time (method
+overwriting is not allowed while a package precompiles). Without this call
+`with_backend(f, BackendGB300())` still selects the backend.
+"""
+function enable!()
+    @eval Muscle begin
+        choose_backend_rule(::typeof(binary_einsum), ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
+        choose_backend_rule(::typeof(binary_einsum!), ::DomainCUDA, ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
+        choose_backend_rule(::typeof(unary_einsum), ::DomainCUDA) = $(BackendGB300)()
+        choose_backend_rule(::typeof(unary_einsum!), ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
+    end
+    return nothing
+end
+
+end # module
