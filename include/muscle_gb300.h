@@ -142,6 +142,20 @@ int mgb_group_execute(mgb_group group, void *workspace,
 int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan);
 int mgb_group_destroy(mgb_group group);
 
+/* ---- contraction without a caller workspace --------------------------------
+ * No counterpart in the reference. For callers that cannot allocate device
+ * memory (a fixed byte budget owned by their own allocator, or a path where a
+ * cudaMalloc and its implicit synchronisation are not acceptable): runs the
+ * plan exactly like mgb_contract, with the workspace taken from a scratch
+ * array of MGB_NOALLOC_SCRATCH_BYTES bytes that the library keeps in the
+ * device memory of every GPU that loads it, until the process exits. Plans
+ * that need more scratch fail with MGB_ERR_WORKSPACE. Calls share the array:
+ * calls that overlap on the GPU race. The first call on a device looks up the
+ * array's address; make it before any stream capture. Allocates nothing.   */
+#define MGB_NOALLOC_SCRATCH_BYTES (32u << 20)
+int mgb_contract_noalloc(mgb_plan plan, const void *A, const void *B, void *C,
+                         void *stream);
+
 /* ---- status ---------------------------------------------------------------*/
 const char *mgb_last_error(void);
 /* Reads and clears the device-side status word written by bounded waits and

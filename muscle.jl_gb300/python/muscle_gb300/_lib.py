@@ -65,6 +65,7 @@ _P = ctypes.POINTER
 SIGNATURES = {
     "mgb_contraction_plan": (_i32, [_P(_vp), _P(TensorDesc), _P(TensorDesc), _P(TensorDesc), _i32, _i32]),
     "mgb_contract": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, _vp]),
+    "mgb_contract_noalloc": (_i32, [_vp, _vp, _vp, _vp, _vp]),
     "mgb_unary_plan": (_i32, [_P(_vp), _P(TensorDesc), _P(TensorDesc)]),
     "mgb_unary": (_i32, [_vp, _vp, _vp, _vp, _u64, _vp]),
     "mgb_permute": (_i32, [_P(TensorDesc), _P(TensorDesc), _vp, _vp, _vp]),
