@@ -146,12 +146,13 @@ def ncu_traffic():
 def cpu_sample(n, slices_target_s, seed=0):
     """Times the CPU oracle on the first rows of A (same columns of B)."""
     import oracle.muscle_ref as ref
+    from muscle_gb300 import workloads as wl
 
     rng = np.random.Generator(np.random.PCG64(seed))
 
     def run(rows):
-        a = np.asfortranarray(ref.loguniform_complex(rng, (rows, 128, 64)))
-        b = np.asfortranarray(ref.loguniform_complex(rng, (64, n, 128)))
+        a = np.asfortranarray(wl.loguniform_complex(rng, (rows, 128, 64)))
+        b = np.asfortranarray(wl.loguniform_complex(rng, (64, n, 128)))
         t0 = time.perf_counter()
         ref.contract(a, ["i", "k1", "k2"], b, ["k2", "j", "k1"], ["i", "j"])
         dt = time.perf_counter() - t0
@@ -221,12 +222,12 @@ def main():
 
     import muscle_gb300 as m
     from muscle_gb300 import _lib
-    import oracle.muscle_ref as ref
+    from muscle_gb300 import workloads as wl
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     n = args.n
-    (a, ia), (b, ib), ic = ref.gen_config3(seed=0, n=n)
+    (a, ia), (b, ib), ic = wl.gen_config3(seed=0, n=n)
     a_h = torch.from_numpy(a).pin_memory()
     b_h = torch.from_numpy(b).pin_memory()
     A = a_h.to(dev)  # column-major strides preserved

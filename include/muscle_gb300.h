@@ -121,10 +121,13 @@ int mgb_plan_workspace_size(mgb_plan plan, uint64_t *bytes);
 int mgb_plan_destroy(mgb_plan plan);
 
 /* ---- grouped (batched) contractions ---------------------------------------
- * Many independent plans executed by one persistent grouped launch per arith-
- * metic class. Operand pointers are device pointers. The group is immutable;
- * the pointer arrays are copied at creation (mgb_group_update may replace
- * them before a later execute, e.g. for a CUDA-graph replay with new data).
+ * Many independent contractions on one stream. Members that share a plan
+ * handle (same shapes, strides, element types and form) run as one batched
+ * launch per kernel, the batch index selecting the member's operand and
+ * output pointers from a device array; other members run one by one. The
+ * group copies the pointer arrays at creation into device memory;
+ * mgb_group_update replaces them (a CUDA-graph replay of mgb_group_execute
+ * then reads the new pointers). Operand pointers are device pointers.
  * The ensemble of a PEPS sweep is the motivating case
  * (ext/MuscleDaggerExt/binary_einsum.jl:64-119 runs such independent pairs
  * as separate tasks).                                                      */
@@ -137,8 +140,10 @@ int mgb_group_update(mgb_group group, const void *const *A,
 int mgb_group_workspace_size(mgb_group group, uint64_t *bytes);
 int mgb_group_execute(mgb_group group, void *workspace,
                       uint64_t workspace_bytes, void *stream);
-/* Tile schedule of the grouped kernel: tile index per shape class. The
- * autotuner (host side) writes it; -1 = built-in heuristic.               */
+/* Tile schedule of the batched tensor-core launches: per member, an index
+ * 0..5 into the rasterisation bands {1, 2, 4, 8, 16, 32} (row tiles walked
+ * together across all column tiles); a bucket takes its first member's
+ * value; -1 = default band (16). Written by the host-side autotuner.      */
 int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan);
 int mgb_group_destroy(mgb_group group);
 

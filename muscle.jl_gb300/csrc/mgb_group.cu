@@ -1,24 +1,79 @@
-// Grouped execution of many independent contraction plans on one stream.
+// Grouped execution of many independent contraction plans.
 //
-// Each plan keeps its own arithmetic form. The group carves one workspace
-// into per-plan slices so that all members can be in flight at once and the
-// whole group can be captured into one CUDA graph by the caller.
+// Members that share a plan (same shapes, strides, element types and form;
+// callers that cache plans by descriptor get this for free) form a bucket. A
+// bucket runs as one batched launch of each kernel of its form: the batch
+// index selects the member, whose operand and output pointers come from a
+// device array instead of a batch stride. A PEPS sweep (thousands of pairs of
+// a handful of shape classes) therefore costs a handful of launches per
+// class, all on one stream, so the caller can capture the group in one CUDA
+// graph. Members that cannot be batched (a plain-form plan that converts its
+// operands, an empty contraction, a plan that is already batched) run one by
+// one through mgb_contract. The workspace is carved into per-bucket and
+// per-member slices.
 #include <algorithm>
-#include <cstring>
+#include <map>
 #include <vector>
 
 #include "mgb_internal.h"
+
+namespace {
+
+struct Bucket {
+    mgb_plan plan = nullptr;        // the shared member plan
+    std::vector<int> members;
+    mgb::ContractionPlan cp;        // batched copy: L = members, pointer arrays
+    void **dptr = nullptr;          // device: A[L], B[L], C[L]
+    uint64_t ws_off = 0;
+};
+
+struct Single {
+    int member;
+    uint64_t ws_off;
+};
+
+const int kBands[6] = {1, 2, 4, 8, 16, 32};
+
+}  // namespace
 
 struct mgb_group_s {
     std::vector<mgb_plan> plans;
     std::vector<const void *> A, B;
     std::vector<void *> C;
-    std::vector<uint64_t> ws_off;
-    std::vector<int32_t> tiles;
+    std::vector<Bucket> buckets;
+    std::vector<Single> singles;
     uint64_t ws_bytes = 0;
 };
 
 using namespace mgb;
+
+static bool batchable(const mgb_plan p) {
+    const ContractionPlan &cp = p->cp;
+    if (cp.L != 1 || cp.K == 0 || cp.M * cp.N == 0) return false;
+    if (cp.form == MGB_FORM_PLAIN && (cp.convert_a || cp.convert_b)) return false;
+    return true;
+}
+
+static int upload(mgb_group g) {
+    for (auto &b : g->buckets) {
+        const size_t n = b.members.size();
+        std::vector<void *> h(3 * n);
+        for (size_t i = 0; i < n; ++i) {
+            const int m = b.members[i];
+            h[i] = const_cast<void *>(g->A[m]);
+            h[n + i] = const_cast<void *>(g->B[m]);
+            h[2 * n + i] = g->C[m];
+        }
+        MGB_CUDA_CHECK(cudaMemcpy(b.dptr, h.data(), 3 * n * sizeof(void *), cudaMemcpyHostToDevice));
+    }
+    return MGB_OK;
+}
+
+static void free_group(mgb_group g) {
+    for (auto &b : g->buckets)
+        if (b.dptr) cudaFree(b.dptr);
+    delete g;
+}
 
 extern "C" {
 
@@ -29,21 +84,64 @@ int mgb_group_create(mgb_group *group, const mgb_plan *plans, int32_t count, con
     if (count < 0 || (count > 0 && (!plans || !A || !B || !C)))
         return fail(MGB_ERR_ARGUMENT, "group: null arrays");
     auto *g = new mgb_group_s();
-    uint64_t off = 0;
+    std::map<mgb_plan, int> index;
     for (int i = 0; i < count; ++i) {
         if (!plans[i] || plans[i]->kind != PlanKind::Contraction) {
-            delete g;
+            free_group(g);
             return fail(MGB_ERR_ARGUMENT, "group: member " + std::to_string(i) + " is not a contraction plan");
         }
         g->plans.push_back(plans[i]);
         g->A.push_back(A[i]);
         g->B.push_back(B[i]);
         g->C.push_back(C[i]);
-        g->ws_off.push_back(off);
-        off += (plans[i]->cp.ws_bytes + 255) & ~uint64_t(255);
+        if (batchable(plans[i])) {
+            auto it = index.find(plans[i]);
+            if (it == index.end()) {
+                index[plans[i]] = (int)g->buckets.size();
+                g->buckets.emplace_back();
+                g->buckets.back().plan = plans[i];
+            }
+            g->buckets[index[plans[i]]].members.push_back(i);
+        } else {
+            g->singles.push_back({i, 0});
+        }
     }
-    g->tiles.assign(count, -1);
+    uint64_t off = 0;
+    for (auto &b : g->buckets) {
+        const int64_t n = (int64_t)b.members.size();
+        if (n > 65535) {
+            free_group(g);
+            return fail(MGB_ERR_UNSUPPORTED, "group: more than 65535 members share one plan");
+        }
+        b.cp = b.plan->cp;
+        b.cp.L = n;
+        b.cp.gl.n = 1;
+        b.cp.gl.ext[0] = n;
+        for (int t = 0; t < 3; ++t) b.cp.gl.str[t][0] = 0;
+        if (b.cp.form != MGB_FORM_PLAIN) ozaki_setup(b.cp);  // workspace for L members
+        else b.cp.ws_bytes = 0;
+        cudaError_t e = cudaMalloc((void **)&b.dptr, 3 * n * sizeof(void *));
+        if (e != cudaSuccess) {
+            b.dptr = nullptr;
+            free_group(g);
+            return cuda_fail(e, "cudaMalloc(group pointer arrays)");
+        }
+        b.cp.pa = (const void *const *)b.dptr;
+        b.cp.pb = (const void *const *)(b.dptr + n);
+        b.cp.pc = b.dptr + 2 * n;
+        b.ws_off = off;
+        off += (b.cp.ws_bytes + 255) & ~uint64_t(255);
+    }
+    for (auto &s : g->singles) {
+        s.ws_off = off;
+        off += (g->plans[s.member]->cp.ws_bytes + 255) & ~uint64_t(255);
+    }
     g->ws_bytes = off;
+    int st = upload(g);
+    if (st) {
+        free_group(g);
+        return st;
+    }
     *group = g;
     return MGB_OK;
 }
@@ -55,7 +153,7 @@ int mgb_group_update(mgb_group group, const void *const *A, const void *const *B
         group->B[i] = B[i];
         group->C[i] = C[i];
     }
-    return MGB_OK;
+    return upload(group);
 }
 
 int mgb_group_workspace_size(mgb_group group, uint64_t *bytes) {
@@ -66,7 +164,10 @@ int mgb_group_workspace_size(mgb_group group, uint64_t *bytes) {
 
 int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan) {
     if (!group || !tile_per_plan) return fail(MGB_ERR_ARGUMENT, "group: null argument");
-    for (size_t i = 0; i < group->plans.size(); ++i) group->tiles[i] = tile_per_plan[i];
+    for (auto &b : group->buckets) {
+        const int t = tile_per_plan[b.members.front()];
+        b.cp.band = (t >= 0 && t < 6) ? kBands[t] : 16;
+    }
     return MGB_OK;
 }
 
@@ -74,17 +175,25 @@ int mgb_group_execute(mgb_group group, void *workspace, uint64_t workspace_bytes
     if (!group) return fail(MGB_ERR_ARGUMENT, "group: null argument");
     if (workspace_bytes < group->ws_bytes || (group->ws_bytes && !workspace))
         return fail(MGB_ERR_WORKSPACE, "group workspace smaller than mgb_group_workspace_size");
-    for (size_t i = 0; i < group->plans.size(); ++i) {
-        void *w = group->ws_bytes ? (char *)workspace + group->ws_off[i] : nullptr;
-        int st = mgb_contract(group->plans[i], group->A[i], group->B[i], group->C[i], w,
-                              group->plans[i]->cp.ws_bytes, stream);
+    cudaStream_t s = (cudaStream_t)stream;
+    for (auto &b : group->buckets) {
+        int st = b.cp.form == MGB_FORM_PLAIN
+                     ? launch_plain_gemm(b.cp, nullptr, nullptr, nullptr, s)
+                     : launch_ozaki(b.cp, nullptr, nullptr, nullptr, (char *)workspace + b.ws_off, s);
+        if (st) return st;
+    }
+    for (auto &m : group->singles) {
+        const mgb_plan p = group->plans[m.member];
+        void *w = p->cp.ws_bytes ? (char *)workspace + m.ws_off : nullptr;
+        int st = mgb_contract(p, group->A[m.member], group->B[m.member], group->C[m.member], w, p->cp.ws_bytes,
+                              stream);
         if (st) return st;
     }
     return MGB_OK;
 }
 
 int mgb_group_destroy(mgb_group group) {
-    delete group;
+    if (group) free_group(group);
     return MGB_OK;
 }
 

@@ -95,6 +95,11 @@ struct ContractionPlan {
     int oz_w = 7;          // slice width in bits
     int oz_kc = 256;       // k-chunk (embedded elements) between exact readouts
     int oz_R = 0;          // -1 when K is too long for the exact accumulator
+    // Grouped execution: per-batch-entry operand / output pointers (device
+    // arrays of L pointers) replace the batch strides when set.
+    const void *const *pa = nullptr, *const *pb = nullptr;
+    void *const *pc = nullptr;
+    int band = 16;         // tensor-core kernel: row tiles per rasterisation band
     uint64_t ws_bytes = 0;
     // workspace layout (byte offsets)
     uint64_t ws_a = 0, ws_b = 0, ws_scale_a = 0, ws_scale_b = 0;

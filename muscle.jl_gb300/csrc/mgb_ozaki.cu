@@ -222,6 +222,7 @@ __host__ __device__ constexpr uint32_t oz_idesc() {
 // =============================================================================
 struct OpGeom {
     ModeGroup gr, gk, gl;  // rows, contracted, batch
+    const void *const *ptrs;  // per-batch-entry base pointers (grouped execution) or null
     int t;                 // tensor index inside the groups (0 = A, 1 = B)
     int64_t R, K;
     int rows_fast;         // operand's unit-stride mode is a row mode
@@ -244,7 +245,7 @@ __global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeo
     int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
     if (tid < 32) roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
     else if (tid < 64) koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
-    const T *Xl = X + group_offset(g.gl, g.t, l);
+    const T *Xl = g.ptrs ? (const T *)g.ptrs[l] : X + group_offset(g.gl, g.t, l);
     __syncthreads();
     if (g.rows_fast) {
         int e = 0;
@@ -378,7 +379,7 @@ __global__ void __launch_bounds__(256) k_oz_slice(const T *__restrict__ X, OpGeo
         }
     }
     if (tid < KT) koff[tid] = (k0 + tid < g.K) ? group_offset(g.gk, g.t, k0 + tid) : 0;
-    const T *Xl = X + group_offset(g.gl, g.t, l);
+    const T *Xl = g.ptrs ? (const T *)g.ptrs[l] : X + group_offset(g.gl, g.t, l);
     __syncthreads();
     for (int idx = tid; idx < 32 * KT; idx += 256) {
         int r, kk;
@@ -470,6 +471,8 @@ struct OzGemmArgs {
     const int32_t *expA;   // [L][M] biased exponents (OZAKI)
     const int32_t *expB;   // [L][N]
     void *C;
+    void *const *cptr;     // per-batch-entry output pointers (grouped execution) or null
+    int32_t band;          // row tiles per rasterisation band
     ModeGroup gm, gn, gl;  // C offsets live in tensor slot 2
     int32_t *status;
 };
@@ -512,10 +515,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     {
         const int64_t nm = gridDim.y, nn = gridDim.x;
         const int64_t t = (int64_t)blockIdx.y * nn + blockIdx.x;
-        const int64_t band = t / (OZ_GROUP_M * nn);
-        const int64_t first = band * OZ_GROUP_M;
-        const int64_t rows = min((int64_t)OZ_GROUP_M, nm - first);
-        const int64_t r = t - band * OZ_GROUP_M * nn;
+        const int64_t gm = args.band;
+        const int64_t band = t / (gm * nn);
+        const int64_t first = band * gm;
+        const int64_t rows = min(gm, nm - first);
+        const int64_t r = t - band * gm * nn;
         m_tile = first + r % rows;
         n_tile = r / rows;
     }
@@ -855,7 +859,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             }
         }
         if (ok && row < args.M) {
-            const int64_t lb = group_offset(args.gl, 2, l);
+            void *const Cl = args.cptr ? args.cptr[l] : args.C;
+            const int64_t lb = args.cptr ? 0 : group_offset(args.gl, 2, l);
             const int64_t om = group_offset(args.gm, 2, row);
             int erow = 0;
             bool badrow = false;
@@ -879,13 +884,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     double v0 = bad ? nan : ldexp(x96_to_double(w0[j], w1[j], w2[j]), E);
                     if (CX) {
                         double v1 = bad ? nan : ldexp(x96_to_double(w0[j + 1], w1[j + 1], w2[j + 1]), E);
-                        ((double2 *)args.C)[off] = make_double2(v0, v1);
+                        ((double2 *)Cl)[off] = make_double2(v0, v1);
                     } else {
-                        ((double *)args.C)[off] = v0;
+                        ((double *)Cl)[off] = v0;
                     }
                 } else {
-                    if (CX) ((float2 *)args.C)[off] = make_float2(accf[j], accf[j + 1]);
-                    else ((float *)args.C)[off] = accf[j];
+                    if (CX) ((float2 *)Cl)[off] = make_float2(accf[j], accf[j + 1]);
+                    else ((float *)Cl)[off] = accf[j];
                 }
             }
         }
@@ -1049,6 +1054,8 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
     if (!status) return fail(MGB_ERR_CUDA, "device status word unavailable");
 
     OpGeom ga, gb;
+    ga.ptrs = p.pa;
+    gb.ptrs = p.pb;
     ga.gr = p.gm; ga.gk = p.gk; ga.gl = p.gl; ga.t = 0; ga.R = p.M; ga.K = p.K;
     ga.rows_fast = unit_row_fast(p.gm, p.gk, 0);
     gb.gr = p.gn; gb.gk = p.gk; gb.gl = p.gl; gb.t = 1; gb.R = p.N; gb.K = p.K;
@@ -1091,6 +1098,8 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
     a.expA = ea;
     a.expB = eb;
     a.C = C;
+    a.cptr = p.pc;
+    a.band = p.band > 0 ? p.band : OZ_GROUP_M;
     a.gm = p.gm;
     a.gn = p.gn;
     a.gl = p.gl;

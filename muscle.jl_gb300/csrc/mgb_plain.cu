@@ -15,6 +15,8 @@ namespace mgb {
 
 struct GemmArgs {
     ModeGroup gm, gn, gk, gl;  // tensor 0 = A, 1 = B, 2 = C
+    const void *const *pa, *const *pb;  // per-batch-entry pointers (grouped execution) or null
+    void *const *pc;
     int64_t M, N, K;
     int a_kfast;  // A's unit-stride mode is contracted (else left)
     int b_kfast;  // B's unit-stride mode is contracted (else right)
@@ -95,9 +97,9 @@ __global__ void __launch_bounds__(128) k_plain_dmma(const T *__restrict__ A, con
 
     const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
     const int64_t l = blockIdx.z;
-    const T *Ab = A + group_offset(g.gl, 0, l);
-    const T *Bb = B + group_offset(g.gl, 1, l);
-    T *Cb = C + group_offset(g.gl, 2, l);
+    const T *Ab = g.pa ? (const T *)g.pa[l] : A + group_offset(g.gl, 0, l);
+    const T *Bb = g.pb ? (const T *)g.pb[l] : B + group_offset(g.gl, 1, l);
+    T *Cb = g.pc ? (T *)g.pc[l] : C + group_offset(g.gl, 2, l);
     int tid = threadIdx.x;
     if (tid < BM) rowA[tid] = (m0 + tid < g.M) ? group_offset(g.gm, 0, m0 + tid) : 0;
     else colB[tid - BM] = (n0 + tid - BM < g.N) ? group_offset(g.gn, 1, n0 + tid - BM) : 0;
@@ -188,9 +190,9 @@ __global__ void __launch_bounds__(256) k_plain_ffma(const T *__restrict__ A, con
     __shared__ int64_t rowA[BM], colB[BN], kA[BK], kB[BK];
     const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
     const int64_t l = blockIdx.z;
-    const T *Ab = A + group_offset(g.gl, 0, l);
-    const T *Bb = B + group_offset(g.gl, 1, l);
-    T *Cb = C + group_offset(g.gl, 2, l);
+    const T *Ab = g.pa ? (const T *)g.pa[l] : A + group_offset(g.gl, 0, l);
+    const T *Bb = g.pb ? (const T *)g.pb[l] : B + group_offset(g.gl, 1, l);
+    T *Cb = g.pc ? (T *)g.pc[l] : C + group_offset(g.gl, 2, l);
     int tid = threadIdx.x;
     if (tid < BM) rowA[tid] = (m0 + tid < g.M) ? group_offset(g.gm, 0, m0 + tid) : 0;
     else if (tid < BM + BN) colB[tid - BM] = (n0 + tid - BM < g.N) ? group_offset(g.gn, 1, n0 + tid - BM) : 0;
@@ -263,6 +265,9 @@ int launch_plain_gemm(const ContractionPlan &p, const void *A, const void *B, vo
     g.M = p.M;
     g.N = p.N;
     g.K = p.K;
+    g.pa = p.pa;
+    g.pb = p.pb;
+    g.pc = p.pc;
     g.a_kfast = unit_stride_in(p.gk, 0) && !unit_stride_in(p.gm, 0);
     g.b_kfast = unit_stride_in(p.gk, 1) && !unit_stride_in(p.gn, 1);
     int64_t gx = (p.N + BN - 1) / BN, gy = (p.M + BM - 1) / BM;

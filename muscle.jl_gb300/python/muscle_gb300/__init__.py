@@ -38,6 +38,7 @@ from .ops import (
     unary_einsum_,
     unary_plan,
 )
+from .grouped import Group, batched_contract
 from .tensor import (
     Index,
     Tensor,

@@ -3,6 +3,7 @@ import numpy as np
 import pytest
 
 from oracle import muscle_ref as ref
+from muscle_gb300 import workloads as wl
 from tests.kat_util import expected_binary, make_array
 
 
@@ -79,13 +80,13 @@ def test_front_end_defaults():
 
 
 def test_generators_are_seeded():
-    (a1, _), (b1, _), _ = ref.gen_config1(seed=0, dim=4)
-    (a2, _), (b2, _), _ = ref.gen_config1(seed=0, dim=4)
+    (a1, _), (b1, _), _ = wl.gen_config1(seed=0, dim=4)
+    (a2, _), (b2, _), _ = wl.gen_config1(seed=0, dim=4)
     assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
-    (a, ia), (b, ib), ic = ref.gen_config3(seed=0, n=64, k1=8, k2=4)
+    (a, ia), (b, ib), ic = wl.gen_config3(seed=0, n=64, k1=8, k2=4)
     mags = np.log2(np.abs(a))
     assert mags.min() >= -20 and mags.max() <= 20
     for s in range(20):
-        (pa, pia), (pb, pib), pic, tries = ref.peps_instance(100 + s)
+        (pa, pia), (pb, pib), pic, tries = wl.peps_instance(100 + s)
         n = pa.size + pb.size + int(np.prod([dict(zip(pia + pib, pa.shape + pb.shape))[i] for i in pic]))
-        assert n <= ref.PEPS_CAP
+        assert n <= wl.PEPS_CAP
