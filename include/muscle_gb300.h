@@ -147,6 +147,40 @@ int mgb_group_execute(mgb_group group, void *workspace,
 int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan);
 int mgb_group_destroy(mgb_group group);
 
+/* ---- serving loop -----------------------------------------------------------
+ * Contractions submitted as they arrive are admitted against a device-memory
+ * byte budget and dispatched with continuous batching onto `nstreams`
+ * streams by a scheduler thread of the library: while earlier batches run,
+ * later arrivals are admitted as budget frees up and launched on the other
+ * streams, so their work overlaps on the GPU. A request's admitted bytes are
+ * the caller-declared resident bytes (operands and output, which stay in
+ * device memory owned by the caller) plus its workspace, which the server
+ * allocates from its own stream-ordered pool. A request larger than the
+ * whole budget finishes at once with MGB_ERR_OUT_OF_MEMORY. `dep_stream`
+ * (may be NULL) is a caller stream whose work so far the request waits for
+ * (e.g. the kernels that produced its operands). Plans and buffers must stay
+ * alive until mgb_server_wait has returned for the ticket. This is the
+ * request loop of the serving form; the reference has no counterpart.     */
+typedef struct mgb_server_s *mgb_server;
+typedef struct mgb_server_stats {
+    uint64_t submitted, completed, rejected, batches, pending, used_bytes;
+    double p50_ms, p99_ms, max_ms;  /* latency: submission -> completion seen */
+    double elapsed_s;               /* since creation or the last reset         */
+} mgb_server_stats;
+int mgb_server_create(mgb_server *server, uint64_t budget_bytes, int32_t nstreams,
+                      int32_t max_batch);
+int mgb_server_submit(mgb_server server, mgb_plan plan, const void *A,
+                      const void *B, void *C, uint64_t resident_bytes,
+                      void *dep_stream, int64_t *ticket);
+/* Blocks until the ticket's request finished (timeout_s < 0: no timeout);
+ * *status is its mgb_status. Each ticket is waited for once.              */
+int mgb_server_wait(mgb_server server, int64_t ticket, double timeout_s,
+                    int32_t *status);
+int mgb_server_get_stats(mgb_server server, mgb_server_stats *stats);
+int mgb_server_reset_stats(mgb_server server);
+/* Waits for queued and running requests, then frees streams and the pool.  */
+int mgb_server_destroy(mgb_server server);
+
 /* ---- contraction without a caller workspace --------------------------------
  * No counterpart in the reference. For callers that cannot allocate device
  * memory (a fixed byte budget owned by their own allocator, or a path where a

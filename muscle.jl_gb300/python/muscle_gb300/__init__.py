@@ -39,6 +39,7 @@ from .ops import (
     unary_plan,
 )
 from .grouped import Group, batched_contract
+from .serve import Request, Server
 from .tensor import (
     Index,
     Tensor,

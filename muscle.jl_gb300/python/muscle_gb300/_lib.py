@@ -61,6 +61,21 @@ class PlanInfo(ctypes.Structure):
     ]
 
 
+class ServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_uint64),
+        ("completed", ctypes.c_uint64),
+        ("rejected", ctypes.c_uint64),
+        ("batches", ctypes.c_uint64),
+        ("pending", ctypes.c_uint64),
+        ("used_bytes", ctypes.c_uint64),
+        ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double),
+        ("max_ms", ctypes.c_double),
+        ("elapsed_s", ctypes.c_double),
+    ]
+
+
 _P = ctypes.POINTER
 SIGNATURES = {
     "mgb_contraction_plan": (_i32, [_P(_vp), _P(TensorDesc), _P(TensorDesc), _P(TensorDesc), _i32, _i32]),
@@ -80,6 +95,12 @@ SIGNATURES = {
     "mgb_group_execute": (_i32, [_vp, _vp, _u64, _vp]),
     "mgb_group_set_tiles": (_i32, [_vp, _P(_i32)]),
     "mgb_group_destroy": (_i32, [_vp]),
+    "mgb_server_create": (_i32, [_P(_vp), _u64, _i32, _i32]),
+    "mgb_server_submit": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, _vp, _P(ctypes.c_int64)]),
+    "mgb_server_wait": (_i32, [_vp, ctypes.c_int64, ctypes.c_double, _P(_i32)]),
+    "mgb_server_get_stats": (_i32, [_vp, _P(ServerStats)]),
+    "mgb_server_reset_stats": (_i32, [_vp]),
+    "mgb_server_destroy": (_i32, [_vp]),
     "mgb_last_error": (ctypes.c_char_p, []),
     "mgb_device_status": (_i32, [_vp, _P(_i32)]),
     "mgb_version": (ctypes.c_char_p, []),

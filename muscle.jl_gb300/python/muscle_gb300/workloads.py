@@ -99,3 +99,49 @@ def peps_instance(seed, dtype=np.complex128, cap=PEPS_CAP, max_tries=1000):
         b = colmajor(_cnormal(rng, eb, dtype, sc))
         return (a, ia), (b, ib), ic, tries
     raise RuntimeError("no instance under the cap")
+
+
+SERVE_DTYPES = (np.complex128, np.float64, np.complex64)
+
+
+def serve_request(rng, flops_lo=1e4, flops_hi=1e10, dtypes=SERVE_DTYPES):
+    """One serving-form request: a random binary contraction with ranks 3-6,
+    1-3 contracted labels, extents drawn so that its algorithmic flops are
+    log-uniform in [flops_lo, flops_hi], labels in random orders, element type
+    drawn from ``dtypes``. Returns (shape_a, ia, shape_b, ib, ic, dtype, flops)."""
+    dtype = dtypes[int(rng.integers(len(dtypes)))]
+    cx = np.issubdtype(dtype, np.complexfloating)
+    target = float(np.exp(rng.uniform(np.log(flops_lo), np.log(flops_hi))))
+    mnk = max(target / (8.0 if cx else 2.0), 1.0)
+    while True:
+        ra, rb = int(rng.integers(3, 7)), int(rng.integers(3, 7))
+        nc = int(rng.integers(1, 4))
+        if nc < ra and nc < rb:
+            break
+    fa, fb = ra - nc, rb - nc
+    frac = rng.dirichlet([4.0, 4.0, 4.0])  # share of log(MNK) for M, N, K
+
+    def split(total, parts):
+        if parts == 0:
+            return []
+        w = rng.dirichlet([2.0] * parts)
+        return [max(1, int(round(total ** wi))) for wi in w]
+
+    em, en, ek = split(mnk ** frac[0], fa), split(mnk ** frac[1], fb), split(mnk ** frac[2], nc)
+    names = [f"x{i}" for i in range(fa + fb + nc)]
+    rng.shuffle(names)
+    lm, ln, lk = names[:fa], names[fa:fa + fb], names[fa + fb:]
+    ext = dict(zip(lm + ln + lk, em + en + ek))
+    ia = list(lm + lk)
+    ib = list(lk + ln)
+    ic = list(lm + ln)
+    for lab in (ia, ib, ic):
+        rng.shuffle(lab)
+    flops = (8.0 if cx else 2.0) * np.prod(em) * np.prod(en) * np.prod(ek)
+    return [ext[i] for i in ia], ia, [ext[i] for i in ib], ib, ic, dtype, float(flops)
+
+
+def serve_arrays(rng, req):
+    """Seeded operands (iid N(0,1), complex parts independent) for a request."""
+    sa, ia, sb, ib, ic, dtype, _ = req
+    return _cnormal(rng, sa, dtype), _cnormal(rng, sb, dtype)
