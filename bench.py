@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--n", type=int, default=8192, help="M = N of the precision workload")
     ap.add_argument("--native-steps", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
+    ap.add_argument("--workload", default="precision", choices=["precision", "peps", "serve"],
+                    help="precision: the headline line; peps / serve: batching and serving forms")
+    ap.add_argument("--serve-seconds", type=float, default=1.5, help="per offered rate in the serving sweep")
+    ap.add_argument("--instances", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -194,6 +198,176 @@ def barrier(ws):
         dist.barrier()
 
 
+# ----------------------------------------------------------------------------- serving
+def _device_requests(n, seed, dev, flops_hi=1e10, mem_cap=24 << 30):
+    """Serving-form requests with device-resident operands (shapes from the
+    seeded generator, values from a seeded device generator). Requests are
+    drawn until n are collected within `mem_cap` bytes in total."""
+    import torch
+
+    import muscle_gb300 as m
+    from muscle_gb300 import workloads as wl
+
+    rng = np.random.default_rng(seed)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    tdt = {np.complex128: torch.complex128, np.float64: torch.float64, np.complex64: torch.complex64}
+    out, used = [], 0
+    while len(out) < n:
+        sa, ia, sb, ib, ic, dt, fl = wl.serve_request(rng, 1e4, flops_hi)
+        ext = dict(zip(ia + ib, sa + sb))
+        t = tdt[dt]
+        nbytes = (np.prod(sa) + np.prod(sb) + np.prod([ext[i] for i in ic])) * torch.empty((), dtype=t).element_size()
+        if used + nbytes > mem_cap:
+            continue
+        used += nbytes
+        A = m.Tensor(torch.randn(list(reversed(sa)), dtype=t, device=dev, generator=gen).permute(*reversed(range(len(sa)))), ia)
+        B = m.Tensor(torch.randn(list(reversed(sb)), dtype=t, device=dev, generator=gen).permute(*reversed(range(len(sb)))), ib)
+        C = m.Tensor(m.empty_colmajor([ext[i] for i in ic], t, dev), ic)
+        out.append((A, B, C, fl))
+    torch.cuda.synchronize(dev)
+    return out
+
+
+def serve_bench(dev, rates, seconds, n_requests=192, seed=5, budget=120 * 10**9, quick=False):
+    """One-at-a-time plain launches versus the served stream (continuous
+    batching, emulated and plain forms) under Poisson arrivals."""
+    import torch
+
+    import muscle_gb300 as m
+
+    reqs = _device_requests(n_requests, seed, dev, mem_cap=(16 << 30) if quick else (48 << 30))
+    res = {"requests_in_pool": len(reqs), "flops_mean": float(np.mean([r[3] for r in reqs]))}
+    # one at a time, plain form: launch, wait, next
+    plans = {}
+    for form in ("plain", "auto"):
+        plans[form] = [m.contraction_plan(A.data, A.inds, B.data, B.inds, C.data, C.inds, form) for A, B, C, _ in reqs]
+    ws = torch.empty(max(max(p.workspace_bytes for p in plans["auto"]), 1), dtype=torch.uint8, device=dev)
+    from muscle_gb300 import _lib
+
+    lib = _lib.load()
+    st = torch.cuda.current_stream(dev).cuda_stream
+    t0 = time.perf_counter()
+    n_done = 0
+    while time.perf_counter() - t0 < (0.5 if quick else 2.0) or n_done < 16:
+        A, B, C, _ = reqs[n_done % len(reqs)]
+        p = plans["plain"][n_done % len(reqs)]
+        _lib.check(lib.mgb_contract(p.handle, A.data.data_ptr(), B.data.data_ptr(), C.data.data_ptr(),
+                                    ws.data_ptr(), ws.numel(), st), lib)
+        torch.cuda.synchronize(dev)
+        n_done += 1
+    serial = n_done / (time.perf_counter() - t0)
+    res["one_at_a_time_plain_per_s"] = serial
+    sweeps = []
+    for form in ("auto", "plain"):
+        # the native FP64 form saturates two orders of magnitude earlier
+        form_rates = rates if form == "auto" else [r / 50.0 for r in rates]
+        with m.Server(budget_bytes=budget, streams=4, max_batch=64, form=form, device=dev) as srv:
+            for rate in form_rates:
+                srv.reset_stats()
+                rng = np.random.default_rng(seed + int(rate))
+                t_start = time.perf_counter()
+                t_next = t_start
+                sent, pend = 0, []
+                overloaded = False
+                while True:
+                    now = time.perf_counter()
+                    if now - t_start >= seconds:
+                        break
+                    if now < t_next:
+                        continue
+                    if sent % 256 == 0 and sent - srv.stats()["completed"] > 4096:
+                        overloaded = True  # backlog beyond 4096 requests: stop offering
+                        break
+                    i = sent % len(reqs)
+                    A, B, C, _ = reqs[i]
+                    pend.append(srv.submit_planned(plans[form][i], A, B, C))
+                    sent += 1
+                    t_next += rng.exponential(1.0 / rate)
+                for q in pend:
+                    q.wait()
+                elapsed = time.perf_counter() - t_start
+                sts = srv.stats()
+                flops = sum(reqs[k % len(reqs)][3] for k in range(sent))
+                sweeps.append({"form": "emulated" if form == "auto" else "plain", "offered_per_s": rate,
+                               "overloaded": overloaded,
+                               "submitted_per_s": sent / seconds, "completed_per_s": sts["completed"] / elapsed,
+                               "tflops": flops / elapsed / 1e12, "p50_ms": sts["p50_ms"], "p99_ms": sts["p99_ms"],
+                               "batches": sts["batches"]})
+    res["sweep"] = sweeps
+    best = max((x for x in sweeps if x["form"] == "emulated" and not x["overloaded"]),
+               key=lambda x: x["completed_per_s"], default=sweeps[0])
+    res["served_emulated_best"] = best
+    res["served_vs_one_at_a_time_plain"] = best["completed_per_s"] / serial
+    return res
+
+
+def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
+    """Batching form: PEPS-style pairs, one group per element type, autotuned
+    schedule, replayed as one CUDA graph."""
+    import torch
+
+    import muscle_gb300 as m
+    from muscle_gb300 import workloads as wl
+    from muscle_gb300.autotune import Autotuner
+
+    out = {"instances": instances, "cap_elements": cap}
+    rng_np = []
+    shapes = []
+    rej = 0
+    for i in range(instances):
+        (a, ia), (b, ib), ic, tries = wl.peps_instance(seed + i, cap=cap, dtype=np.complex64)
+        shapes.append((a.shape, ia, b.shape, ib, ic))
+        rej += tries - 1
+    out["redraws_per_instance"] = rej / instances
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    for tdt in (torch.complex128, torch.complex64):
+        items, flops = [], 0.0
+        for sa, ia, sb, ib, ic in shapes:
+            chi = sa[1]
+            sc = (1.0 / chi) ** 0.5
+            A = m.Tensor((torch.randn(list(reversed(sa)), dtype=tdt, device=dev, generator=gen) * sc).permute(4, 3, 2, 1, 0), ia)
+            B = m.Tensor((torch.randn(list(reversed(sb)), dtype=tdt, device=dev, generator=gen) * sc).permute(4, 3, 2, 1, 0), ib)
+            ext = dict(zip(ia + ib, sa + sb))
+            C = m.Tensor(m.empty_colmajor([ext[x] for x in ic], tdt, dev), ic)
+            items.append((C, A, B))
+        tuner = Autotuner(os.path.join(ROOT, "gpurun_out", "autotune_peps.json") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else None, reps=2)
+        g = tuner.group(items)
+        flops = g.flops
+        graph = g.capture()
+        for _ in range(3):
+            graph.replay()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            graph.replay()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        # one at a time, plain form, on the first 256 instances
+        sub = items[:256]
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for C, A, B in sub:
+            with m.with_backend(m.BackendGB300("plain")):
+                m.binary_einsum_(C, A, B)
+            torch.cuda.synchronize(dev)
+        one = len(sub) / (time.perf_counter() - t0)
+        forms = {}
+        for f in g.forms:
+            forms[f] = forms.get(f, 0) + 1
+        key = "c64" if tdt == torch.complex128 else "c32"
+        out[key] = {"graph_ms": ms, "tflops": flops / (ms / 1e3) / 1e12, "contractions_per_s": len(items) / (ms / 1e3),
+                    "one_at_a_time_plain_per_s": one, "forms_chosen": forms, "gflop": flops / 1e9,
+                    "distinct_plans": len({id(p) for p in g.plans})}
+        del g, graph, items
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -226,6 +400,16 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.workload != "precision":
+        if args.workload == "peps":
+            res = peps_bench(dev, args.instances)
+            metric = "PEPS batch: contractions/s and TFLOP/s, one graph-captured group"
+        else:
+            res = serve_bench(dev, [1000, 3000, 10000, 30000, 100000], args.serve_seconds)
+            metric = "served contractions/s with p50/p99 ms (Poisson arrivals)"
+        if rank == 0:
+            print(json.dumps({"metric": metric, "workload": args.workload, "n_gpus": ws, **res}), flush=True)
+        return
     n = args.n
     (a, ia), (b, ib), ic = wl.gen_config3(seed=0, n=n)
     a_h = torch.from_numpy(a).pin_memory()
@@ -320,6 +504,10 @@ def main():
     e2e = flops * ws * args.steps / (e2e_ms / 1e3) / 1e12
     status = m.device_status(dev)
 
+    # served mixed-size stream (short sweep; the full one is --workload serve)
+    del a_h, b_h, c_h
+    serving = serve_bench(dev, [1000, 10000, 100000], 1.0, n_requests=64, quick=True)
+
     cpu = None
     if rank == 0 and ws == 1:
         cpu = cpu_sample(n, args.cpu_seconds)
@@ -339,6 +527,13 @@ def main():
                          "frac": achieved / bf16_peak, "traffic": traffic, "peak_kind": f"bf16 dense burst ({peak_kind})",
                          "kernel": "k_oz_gemm", "kernel_ms": gemm_ms, "prepass_ms": statistics.mean(pre),
                          "work": f"2 x {pairs} slice pairs x M x 2N x 2K bf16 flops per launch"},
+            "serving": {"p50_ms": serving["served_emulated_best"]["p50_ms"],
+                        "p99_ms": serving["served_emulated_best"]["p99_ms"],
+                        "completed_per_s": serving["served_emulated_best"]["completed_per_s"],
+                        "offered_per_s": serving["served_emulated_best"]["offered_per_s"],
+                        "one_at_a_time_plain_per_s": serving["one_at_a_time_plain_per_s"],
+                        "ratio_vs_one_at_a_time_plain": serving["served_vs_one_at_a_time_plain"],
+                        "sweep": serving["sweep"]},
             "gpu_launches": launches_per_step * args.steps,
             "device_status": status,
             "clocks": clk.summary(),
