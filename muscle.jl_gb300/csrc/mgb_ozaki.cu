@@ -4,20 +4,26 @@
 //   Each row m of A and column n of B gets a power-of-two scale from its
 //   largest exponent; the scaled value a in [-1, 1] is cut into S signed
 //   W-bit digits by round-to-nearest:  a = sum_i s_i 2^(-W i) + r,
-//   |s_1| <= 2^W, |s_i| <= 2^(W-1), |r| <= 2^(-W S - 1).  With W = 7 every
-//   digit is an integer that bf16 holds exactly, every digit product is
-//   exact, and a float32 accumulator stays exact while the sum of the
-//   absolute products it receives is <= 2^24.  Products s_i t_j with
-//   i + j = d share the scale 2^(-W d) and go to one TMEM accumulator per d
-//   ("group"); pairs with i + j > S + 1 are dropped (Ozaki scheme I).
-//   Every KC = 256 embedded k the epilogue warps read each group's float32
-//   partial sums (exact integers), convert them to int and add them, shifted
-//   left by W (S + 1 - d), into one exact 96-bit integer per output element
+//   |s_1| <= 2^W, |s_i| <= 2^(W-1), |r| <= 2^(-W S - 1).  W = 8 for S <= 6
+//   and W = 7 for S >= 7: every digit is an integer that bf16 holds exactly,
+//   every digit product is exact, and a float32 accumulator stays exact
+//   while the sum of the absolute products it receives is <= 2^24.
+//   Products s_i t_j with i + j = d share the scale 2^(-W d) and go to one
+//   TMEM accumulator per d ("group"); pairs with i + j > S + 1 are dropped
+//   (Ozaki scheme I).  Every KC embedded k (KC = 256 for W = 7, 128 for
+//   W = 8) the epilogue warps read each group's float32 partial sums (exact
+//   integers), convert them to int and add them, shifted left by
+//   W (S + 1 - d), into one exact 96-bit integer per output element
 //   (|X| < 2^(log2 K + W (S + 1) + 1) < 2^95 for any K below 2^31). The only
 //   float64 arithmetic left is the conversion of X and one ldexp per output
 //   element (GB300's FP64 pipe is slow).
 //   Group bound per k: max(d + 1, 4) * 2^(2W-2); KC * bound <= 2^24 for
-//   d <= 15, so the readout is exact for every S <= 8 supported here.
+//   d <= 15 (W = 7) and d <= 7 (W = 8), which covers every group of every
+//   supported S (d <= S + 1).  The chunk boundaries of the groups are
+//   staggered by one k block each, so at most ceil(groups / chunk blocks)
+//   groups are being read out at any time; that many spare TMEM
+//   accumulators rotate through the groups and the MMA issuer never waits
+//   for a readout in the middle of a k block.
 //
 // BF16X3 (Float32 / ComplexF32 results)
 //   x = hi + mid + lo, three bf16 pieces (exact for normal floats); the six
@@ -51,8 +57,7 @@
 
 namespace mgb {
 
-constexpr int OZ_W = 7;        // digit width (bits)
-constexpr int OZ_KC = 256;     // embedded k between exact readouts
+constexpr int OZ_KC = 256;     // BF16X3: embedded k between readouts
 constexpr int OZ_BM = 128;     // rows of A per CTA (TMEM lanes)
 constexpr int OZ_BN = 64;      // embedded rows of B per CTA
 constexpr int OZ_BK = 32;      // k per stage (64-byte swizzled rows)
@@ -65,6 +70,13 @@ constexpr int OZ_SMEM_BUDGET = 200 * 1024;
 constexpr long long OZ_TIMEOUT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 __host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (OZ_A_TILE + OZ_B_TILE); }
+// Digit width and exact chunk length (in 32-wide k blocks) per slice count.
+// W = 8 for S <= 6: |s1| <= 256, |si| <= 128, group bound max(d+1,4) 2^14, so a
+// float32 accumulator stays exact over 4 blocks (128 k) for every d <= 7.
+// W = 7 for S >= 7: group bound max(d+1,4) 2^12, exact over 8 blocks (256 k)
+// for d <= 15. Both hold about the same number of mantissa bits (W S = 48 / 49).
+__host__ __device__ constexpr int oz_digit_bits(int S) { return S <= 6 ? 8 : 7; }
+__host__ __device__ constexpr int oz_chunk_blocks(int S) { return oz_digit_bits(S) == 8 ? 4 : 8; }
 __host__ __device__ constexpr int oz_stages(int S) {
     return (OZ_SMEM_BUDGET / oz_stage_bytes(S)) < 4 ? (OZ_SMEM_BUDGET / oz_stage_bytes(S)) : 4;
 }
@@ -291,7 +303,7 @@ __device__ __forceinline__ uint32_t bf16_bits_of_int(int d) {
 __device__ __forceinline__ uint32_t pack2(uint32_t lo, uint32_t hi) { return lo | (hi << 16); }
 
 // Signed round-to-nearest digits of x * 2^(-e) in 62-bit fixed point.
-__device__ __forceinline__ void oz_digits(double x, int e, int S, int (&d)[8]) {
+__device__ __forceinline__ void oz_digits(double x, int e, int S, int W, int (&d)[8]) {
     uint64_t b = (uint64_t)__double_as_longlong(x);
     int be = (int)((b >> 52) & 0x7FF);
     int64_t m = (int64_t)(b & 0xFFFFFFFFFFFFFull);
@@ -310,7 +322,7 @@ __device__ __forceinline__ void oz_digits(double x, int e, int S, int (&d)[8]) {
     if (b >> 63) Q = -Q;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
-        int shift = 62 - OZ_W * (s + 1);
+        int shift = 62 - W * (s + 1);
         int64_t dig = (Q + ((int64_t)1 << (shift - 1))) >> shift;
         Q -= dig << shift;
         d[s] = s < S ? (int)dig : 0;
@@ -359,7 +371,7 @@ struct OzIn<float2> {
 // BF3 = true: float inputs split into bf16 pieces; otherwise Ozaki digits.
 template <typename T, int MODE, bool BF3>
 __global__ void __launch_bounds__(256) k_oz_slice(const T *__restrict__ X, OpGeom g,
-                                                  const int32_t *__restrict__ exps, int S,
+                                                  const int32_t *__restrict__ exps, int S, int W,
                                                   uint32_t *__restrict__ out, int64_t rows_e,
                                                   int64_t kw) {
     constexpr int KT = MODE == MODE_REAL ? 64 : 32;  // k per tile
@@ -413,8 +425,8 @@ __global__ void __launch_bounds__(256) k_oz_slice(const T *__restrict__ X, OpGeo
                 bf3_pieces((float)OzIn<T>::re(tile[r][2 * tx + 1]), p1);
             } else {
                 int d0[8], d1[8];
-                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx]), bad ? 0 : e, S, d0);
-                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx + 1]), bad ? 0 : e, S, d1);
+                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx]), bad ? 0 : e, S, W, d0);
+                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx + 1]), bad ? 0 : e, S, W, d1);
 #pragma unroll
                 for (int s = 0; s < 8; ++s) {
                     p0[s] = bf16_bits_of_int(d0[s]);
@@ -435,8 +447,8 @@ __global__ void __launch_bounds__(256) k_oz_slice(const T *__restrict__ X, OpGeo
                 bf3_pieces(nim, pn);
             } else {
                 int dr[8], di[8];
-                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][tx]), bad ? 0 : e, S, dr);
-                oz_digits(bad ? 0.0 : (double)OzIn<T>::im(tile[r][tx]), bad ? 0 : e, S, di);
+                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][tx]), bad ? 0 : e, S, W, dr);
+                oz_digits(bad ? 0.0 : (double)OzIn<T>::im(tile[r][tx]), bad ? 0 : e, S, W, di);
 #pragma unroll
                 for (int s = 0; s < 8; ++s) {
                     pr[s] = bf16_bits_of_int(dr[s]);
@@ -485,10 +497,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     // double-buffers them so the MMA never waits for the readout.
     constexpr int NG = EXACT ? S : 2;
     constexpr int NB = EXACT ? 1 : 2;
-    // ROT: one spare accumulator slot; a digit group whose chunk ends moves to
-    // the free slot and leaves the old one to the epilogue (S <= 7 fits TMEM).
-    constexpr bool ROT = EXACT && S <= 7;
-    constexpr int NSLOT = ROT ? S + 1 : NG * NB;
+    constexpr int W = oz_digit_bits(S);     // digit width (EXACT)
+    constexpr int KCB = oz_chunk_blocks(S); // exact chunk length in k blocks (EXACT)
+    // ROT: spare accumulator slots; a digit group whose chunk ends moves to a
+    // free slot and leaves the old one to the epilogue. Up to ceil(NG / KCB)
+    // groups end together, so that many spares are needed (S <= 7 fits TMEM).
+    constexpr int NSPARE = (NG + KCB - 1) / KCB;
+    constexpr bool ROT = EXACT && NG + NSPARE <= 8;
+    constexpr int NSLOT = ROT ? NG + NSPARE : NG * NB;
     constexpr int NST = oz_stages(S);
     constexpr int STAGE = oz_stage_bytes(S);
     constexpr int TCOLS = oz_tmem_cols(NSLOT);
@@ -577,10 +593,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             const uint32_t idesc = oz_idesc();
             bool ok = true;
             if constexpr (ROT) {
-                // slot of group g: 4 bits of `map`; `freeslot` holds the spare one
-                uint32_t map = 0, freeslot = S, fill = 0;  // fill bit x: parity of chunks left in slot x
+                // Group g closes a chunk after k block kb when g % KCB == (kb + 1) % KCB.
+                // slot of group g: 4 bits of `map`; free slots: FIFO of 4-bit ids in fq
+                uint32_t map = 0, fq = 0, fill = 0;  // fill bit x: parity of chunks left in slot x
 #pragma unroll
-                for (int g = 0; g < S; ++g) map |= (uint32_t)g << (4 * g);
+                for (int g = 0; g < NG; ++g) map |= (uint32_t)g << (4 * g);
+#pragma unroll
+                for (int x = NG; x < NSLOT; ++x) fq |= (uint32_t)x << (4 * (x - NG));
                 for (int kb = 0; kb < nkb && ok; ++kb) {
                     const int s = kb % NST;
                     const uint32_t round = kb / NST;
@@ -588,13 +607,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                         ok = false;
                         break;
                     }
-                    const int gs = kb == 0 ? -1 : kb % kcb;  // group starting a new chunk
-                    if (gs >= 0 && gs < S) {
-                        const uint32_t nw = freeslot;
-                        freeslot = (map >> (4 * gs)) & 15u;
-                        map = (map & ~(15u << (4 * gs))) | (nw << (4 * gs));
-                        // the chunk previously left in slot nw must have been read out
-                        ok = mbar_wait(smem_u32(acc_empty + nw), ((fill >> nw) & 1u) ^ 1u, abort_flag, args.status);
+                    const int r = kb % KCB;  // groups g % KCB == r start a new chunk (kb > 0)
+                    if (kb > 0) {
+                        for (int g = r; g < NG && ok; g += KCB) {
+                            const uint32_t nw = fq & 15u;
+                            const uint32_t old = (map >> (4 * g)) & 15u;
+                            fq = (fq >> 4) | (old << (4 * (NSPARE - 1)));
+                            map = (map & ~(15u << (4 * g))) | (nw << (4 * g));
+                            // the chunk previously left in slot nw must have been read out
+                            ok = mbar_wait(smem_u32(acc_empty + nw), ((fill >> nw) & 1u) ^ 1u, abort_flag,
+                                           args.status);
+                        }
                         if (!ok) break;
                     }
                     tc_fence_after();
@@ -609,17 +632,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                             for (int j = 0; j < S - i; ++j) {
                                 const int g = i + j;
                                 const uint32_t d = tmem + ((map >> (4 * g)) & 15u) * OZ_BN;
-                                const uint32_t acc = (k16 == 0 && i == 0 && (kb == 0 || g == gs)) ? 0u : 1u;
+                                const uint32_t acc = (k16 == 0 && i == 0 && (kb == 0 || g % KCB == r)) ? 0u : 1u;
                                 tc_mma_if(1u, d, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
                                           bd0 + (uint64_t)((j * OZ_B_TILE + k16 * 32) >> 4), idesc, acc);
                             }
                     tc_commit(smem_u32(empty + s));
                     if (kb == nkb - 1) {
                         for (int g = 0; g < NG; ++g) tc_commit(smem_u32(acc_full + g));
-                    } else if ((kb + 1) % kcb < S) {
-                        const int ge = (kb + 1) % kcb;  // group whose chunk ends here
-                        tc_commit(smem_u32(acc_full + ge));
-                        fill ^= 1u << ((map >> (4 * ge)) & 15u);
+                    } else {
+                        for (int g = (kb + 1) % KCB; g < NG; g += KCB) {  // groups whose chunk ends here
+                            tc_commit(smem_u32(acc_full + g));
+                            fill ^= 1u << ((map >> (4 * g)) & 15u);
+                        }
                     }
                 }
             } else if constexpr (EXACT) {
@@ -751,15 +775,30 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         }
         bool ok = true;
         if constexpr (ROT) {
-            // Same events as below; the slot of each group follows the MMA side's map.
-            uint32_t map = 0, freeslot = S, par = 0;
+            // Readout events in order: after k block kb < nkb - 1 the groups with
+            // g % KCB == (kb + 1) % KCB close a chunk; after the last block every
+            // group closes its last one. Slots follow the MMA side's map and queue.
+            uint32_t map = 0, fq = 0, par = 0;
 #pragma unroll
-            for (int g = 0; g < S; ++g) map |= (uint32_t)g << (4 * g);
-            const int nev = nkb - 1 + NG;
-#pragma unroll 1
-            for (int e = 0; e < nev; ++e) {
-                const int g = e < nkb - 1 ? (e + 1) % kcb : e - (nkb - 1);
-                if (g >= NG) continue;
+            for (int g = 0; g < NG; ++g) map |= (uint32_t)g << (4 * g);
+#pragma unroll
+            for (int x = NG; x < NSLOT; ++x) fq |= (uint32_t)x << (4 * (x - NG));
+            int kb = 0, g = (nkb > 1) ? 1 % KCB : 0;
+            bool last = nkb == 1;
+            while (ok) {
+                // next event (kb, g): skip block boundaries without a closing group
+                if (!last) {
+                    while (g >= NG) {
+                        ++kb;
+                        if (kb == nkb - 1) {
+                            last = true;
+                            g = 0;
+                            break;
+                        }
+                        g = (kb + 1) % KCB;
+                    }
+                }
+                if (last && g >= NG) break;
                 const uint32_t x = (map >> (4 * g)) & 15u;
                 if (!mbar_wait(smem_u32(acc_full + g), (par >> g) & 1, abort_flag, args.status)) {
                     ok = false;
@@ -772,12 +811,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(acc_empty + x));
-                if (e < nkb - 1) {  // group g continues in the free slot
-                    const uint32_t nw = freeslot;
-                    freeslot = x;
+                if (!last) {  // group g continues in the oldest free slot
+                    const uint32_t nw = fq & 15u;
+                    fq = (fq >> 4) | (x << (4 * (NSPARE - 1)));
                     map = (map & ~(15u << (4 * g))) | (nw << (4 * g));
                 }
-                const int sh = OZ_W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
+                const int sh = W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
                 if (sh < 32) {
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
@@ -792,6 +831,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                         add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
                     }
                 }
+                g += last ? 1 : KCB;
             }
         } else if constexpr (EXACT) {
             // Readout events in order: after k block kb < nkb - 1 group
@@ -814,7 +854,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(acc_empty + g));
-                const int sh = OZ_W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
+                const int sh = W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
                 if (sh < 32) {
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
@@ -879,7 +919,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     int bc = args.expB[(int64_t)l * args.N + n];
                     bool bad = badrow || bc == 0x7FF;
                     int ecol = bc == 0 ? -1022 : bc - 1022;
-                    const int E = erow + ecol - OZ_W * (S + 1);
+                    const int E = erow + ecol - W * (S + 1);
                     const double nan = __longlong_as_double(0x7FF8000000000000LL);
                     double v0 = bad ? nan : ldexp(x96_to_double(w0[j], w1[j], w2[j]), E);
                     if (CX) {
@@ -916,8 +956,8 @@ void ozaki_setup(ContractionPlan &p) {
     p.n_e = cx ? 2 * p.N : p.N;
     p.k_e = cx ? 2 * p.K : p.K;
     p.kpad = (p.k_e + 7) / 8 * 8;
-    p.oz_w = OZ_W;
-    p.oz_kc = OZ_KC;
+    p.oz_w = oz_digit_bits(S);
+    p.oz_kc = p.form == MGB_FORM_OZAKI ? 32 * oz_chunk_blocks(S) : OZ_KC;
     uint64_t off = 0;
     p.ws_a = off;
     off = align256(off + (uint64_t)p.L * S * p.m_e * p.kpad * 2);
@@ -929,7 +969,7 @@ void ozaki_setup(ContractionPlan &p) {
         p.ws_scale_b = off;
         off = align256(off + (uint64_t)p.L * p.N * 4);
         // |X| <= k_e * 2^(2W) * 2^(W(S-1)) * (1 + small) must stay below 2^95
-        double xb = std::log2((double)std::max<int64_t>(p.k_e, 1)) + 2 * OZ_W + OZ_W * (S - 1) + 1;
+        double xb = std::log2((double)std::max<int64_t>(p.k_e, 1)) + 2 * p.oz_w + p.oz_w * (S - 1) + 1;
         p.oz_R = xb < 94 ? 0 : -1;  // -1: K too long for the exact accumulator
     }
     p.ws_bytes = off;
@@ -1022,9 +1062,9 @@ static int run_prepass(const OpGeom &g, int mode, const void *X, int32_t *exps, 
     dim3 grid((unsigned)tiles, (unsigned)L);
     const T *x = (const T *)X;
     switch (mode) {
-    case MODE_REAL: k_oz_slice<T, MODE_REAL, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, out, rows_e, kw); break;
-    case MODE_CA: k_oz_slice<T, MODE_CA, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, out, rows_e, kw); break;
-    default: k_oz_slice<T, MODE_CB, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, out, rows_e, kw); break;
+    case MODE_REAL: k_oz_slice<T, MODE_REAL, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw); break;
+    case MODE_CA: k_oz_slice<T, MODE_CA, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw); break;
+    default: k_oz_slice<T, MODE_CB, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw); break;
     }
     MGB_CUDA_CHECK(cudaGetLastError());
     return MGB_OK;
@@ -1093,7 +1133,7 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
     a.Ne = p.n_e;
     a.N = p.N;
     a.nkb = (int32_t)((p.k_e + OZ_BK - 1) / OZ_BK);
-    a.kcb = OZ_KC / OZ_BK;
+    a.kcb = exact ? oz_chunk_blocks(S) : OZ_KC / OZ_BK;
     a.S = S;
     a.expA = ea;
     a.expB = eb;
