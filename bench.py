@@ -52,12 +52,18 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--slices", type=int, default=7)
+    ap.add_argument("--slices", type=int, default=0,
+                    help="Ozaki slice count of the headline; 0: the fastest of the 5..8 sweep within 1e-13")
     ap.add_argument("--n", type=int, default=8192, help="M = N of the precision workload")
     ap.add_argument("--native-steps", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
-    ap.add_argument("--workload", default="precision", choices=["precision", "peps", "serve"],
-                    help="precision: the headline line; peps / serve: batching and serving forms")
+    ap.add_argument("--workload", default="precision",
+                    choices=["precision", "peps", "serve", "config2", "kernel", "permute"],
+                    help="precision: the headline line; peps / serve: batching and serving forms; config2: "
+                         "plain shapes that permute; kernel / permute: one contraction of the precision "
+                         "workload at --n / the permutation of A(a,b,c,d,e) with e = --perm-e (profiling cases)")
+    ap.add_argument("--form", default="ozaki", help="form of --workload kernel")
+    ap.add_argument("--perm-e", type=int, default=32, help="extent of label e in --workload permute")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="per offered rate in the serving sweep")
     ap.add_argument("--instances", type=int, default=4096)
     return ap.parse_args()
@@ -135,12 +141,14 @@ def peaks():
         return 1900.0, 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the Ozaki GEMM from the committed ncu summary."""
+def ncu_traffic(slices):
+    """DRAM bytes per launch of the Ozaki GEMM at `slices` slices, from the
+    committed ncu summary (lines `traffic_bytes_per_full_launch S=<s>: <bytes>`)."""
     path = os.path.join(ROOT, "profiles", "ozaki_gemm_c64_8192.md")
+    key = f"traffic_bytes_per_full_launch S={slices}:"
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_full_launch:"):
+            if line.startswith(key):
                 return float(line.split(":", 1)[1])
     except OSError:
         pass
@@ -332,8 +340,7 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
             ext = dict(zip(ia + ib, sa + sb))
             C = m.Tensor(m.empty_colmajor([ext[x] for x in ic], tdt, dev), ic)
             items.append((C, A, B))
-        tuner = Autotuner(os.path.join(ROOT, "gpurun_out", "autotune_peps.json") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else None, reps=2)
+        tuner = Autotuner(os.environ.get("MGB_AUTOTUNE_CACHE"), reps=2)
         g = tuner.group(items)
         flops = g.flops
         graph = g.capture()
@@ -366,6 +373,154 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
         del g, graph, items
         torch.cuda.empty_cache()
     return out
+
+
+def config2_bench(dev, steps=3):
+    """Plain native FP64/ComplexF64 contractions with index orders that force
+    permutation: (2a) A(a,b,c,d,e) 64x96x64x48x32, B(e,c,f,a) 32x64x128x64 -> (b,d,f);
+    (2b) MPS bond A(l,p,r) 512x4x512, B(r,q,s) 512x4x512 -> (l,p,q,s). Reports the
+    permutation kernel's HBM bandwidth on 2a's A (the permute BackendBase does)
+    and each form's time; the plain form reads the strided operands directly."""
+    import ctypes
+
+    import torch
+
+    import muscle_gb300 as m
+    from muscle_gb300 import _lib
+
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(0)
+    res = {}
+    cases = {"2a": (["a", "b", "c", "d", "e"], [64, 96, 64, 48, 32], ["e", "c", "f", "a"], [32, 64, 128, 64],
+                    ["b", "d", "f"]),
+             "2b": (["l", "p", "r"], [512, 4, 512], ["r", "q", "s"], [512, 4, 512], ["l", "p", "q", "s"])}
+
+    def colmajor_randn(shape, dt):
+        return torch.randn(list(reversed(shape)), dtype=dt, device=dev, generator=gen).permute(
+            *reversed(range(len(shape))))
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps
+
+    for name, (ia, ea, ib, eb, ic) in cases.items():
+        for tdt in (torch.complex128, torch.float64):
+            A = m.Tensor(colmajor_randn(ea, tdt), ia)
+            B = m.Tensor(colmajor_randn(eb, tdt), ib)
+            ext = dict(zip(ia + ib, ea + eb))
+            row = {}
+            outs = {}
+            for form in ("plain", "ozaki"):
+                C = m.Tensor(m.empty_colmajor([ext[i] for i in ic], tdt, dev), ic)
+                plan = m.contraction_plan(A.data, A.inds, B.data, B.inds, C.data, C.inds, form, 7)
+                ws = torch.empty(max(plan.workspace_bytes, 1), dtype=torch.uint8, device=dev)
+
+                def run(plan=plan, C=C, ws=ws):
+                    _lib.check(lib.mgb_contract(plan.handle, A.data.data_ptr(), B.data.data_ptr(), C.data.data_ptr(),
+                                                ws.data_ptr(), ws.numel(), stream.cuda_stream), lib)
+
+                ms = timed(run, 1 if (form == "plain" and name == "2a") else steps)
+                row[form] = {"ms": ms, "tflops": plan.flops / (ms / 1e3) / 1e12}
+                outs[form] = C.data
+                del ws
+            row["rel_err_ozaki_vs_plain"] = (torch.linalg.vector_norm((outs["ozaki"] - outs["plain"]).flatten()) /
+                                             torch.linalg.vector_norm(outs["plain"].flatten())).item()
+            if name == "2a":
+                # the permutation BackendBase stages: A(a,b,c,d,e) -> (b,d,a,c,e)
+                perm = ["b", "d", "a", "c", "e"]
+                Y = m.empty_colmajor([ext[i] for i in perm], tdt, dev)
+                modes = {lab: k for k, lab in enumerate(A.inds)}
+                (xd, kx) = _lib.make_desc(*m.ops._desc_args(A.data, A.inds, modes))
+                (yd, ky) = _lib.make_desc(_lib.C64 if tdt == torch.complex128 else _lib.F64,
+                                          tuple(modes[m.Index(i)] for i in perm), tuple(Y.shape), tuple(Y.stride()))
+
+                def perm_run():
+                    _lib.check(lib.mgb_permute(ctypes.byref(xd), ctypes.byref(yd), A.data.data_ptr(), Y.data_ptr(),
+                                               stream.cuda_stream), lib)
+
+                ms = timed(perm_run, steps)
+                nbytes = 2 * A.data.numel() * A.data.element_size()
+                _, hbm, kind = peaks()
+                row["permute"] = {"ms": ms, "gbs": nbytes / (ms / 1e3) / 1e9, "bytes": nbytes,
+                                  "frac_of_hbm": nbytes / (ms / 1e3) / 1e9 / hbm, "peak_kind": kind}
+                del Y
+            res[f"{name}_{'c64' if tdt == torch.complex128 else 'f64'}"] = row
+            del A, B, outs
+            torch.cuda.empty_cache()
+    return res
+
+
+def kernel_case(dev, n, form, slices, steps, warmup):
+    """One contraction of the precision workload at M = N = n (K = 8192),
+    launched warmup + steps times; phase timing from the plan."""
+    import ctypes
+
+    import torch
+
+    import muscle_gb300 as m
+    from muscle_gb300 import _lib
+    from muscle_gb300 import workloads as wl
+
+    (a, ia), (b, ib), ic = wl.gen_config3(seed=0, n=n)
+    A = torch.from_numpy(a).to(dev)
+    B = torch.from_numpy(b).to(dev)
+    del a, b
+    C = m.empty_colmajor([n, n], torch.complex128, dev)
+    idx = [[m.Index(x) for x in ls] for ls in (ia, ib, ic)]
+    p = m.contraction_plan(A, idx[0], B, idx[1], C, idx[2], form, slices)
+    ws = torch.empty(max(p.workspace_bytes, 1), dtype=torch.uint8, device=dev)
+    lib = _lib.load()
+    st = torch.cuda.current_stream(dev).cuda_stream
+    lib.mgb_plan_set_timing(p.handle, 1)
+    pre, main = [], []
+    for r in range(warmup + steps):
+        _lib.check(lib.mgb_contract(p.handle, A.data_ptr(), B.data_ptr(), C.data_ptr(), ws.data_ptr(), ws.numel(),
+                                    st), lib)
+        fp, fm = ctypes.c_float(), ctypes.c_float()
+        _lib.check(lib.mgb_plan_timing(p.handle, ctypes.byref(fp), ctypes.byref(fm)), lib)
+        if r >= warmup:
+            pre.append(fp.value)
+            main.append(fm.value)
+    ms = statistics.mean(main)
+    return {"n": n, "form": form, "slices": slices, "prepass_ms": statistics.mean(pre), "main_ms": ms,
+            "tflops_alg": p.flops / ((statistics.mean(pre) + ms) / 1e3) / 1e12, "status": m.device_status(dev)}
+
+
+def permute_case(dev, e, steps, warmup):
+    """Permutation of A(a,b,c,d,e) = 64x96x64x48xe ComplexF64 to (b,d,a,c,e), the
+    reordering the host backend stages for the permuting plain shapes."""
+    import torch
+
+    import muscle_gb300 as m
+
+    ia, ea = ["a", "b", "c", "d", "e"], [64, 96, 64, 48, e]
+    perm = ["b", "d", "a", "c", "e"]
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    x = torch.randn(list(reversed(ea)), dtype=torch.complex128, device=dev, generator=g).permute(4, 3, 2, 1, 0)
+    X = m.Tensor(x, ia)
+    for _ in range(warmup):
+        Y = m.permutedims(X, perm)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        Y = m.permutedims(X, perm)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    nb = 2 * x.numel() * x.element_size()
+    return {"bytes": nb, "ms": ms, "gbs": nb / (ms / 1e3) / 1e9,
+            "bit_exact": bool(torch.equal(Y.data, x.permute(1, 3, 0, 2, 4)))}
 
 
 def run_reference(args, ws, rank):
@@ -404,6 +559,15 @@ def main():
         if args.workload == "peps":
             res = peps_bench(dev, args.instances)
             metric = "PEPS batch: contractions/s and TFLOP/s, one graph-captured group"
+        elif args.workload == "config2":
+            res = config2_bench(dev)
+            metric = "plain vs emulated TFLOP/s on permuting shapes; permutation kernel GB/s"
+        elif args.workload == "kernel":
+            res = kernel_case(dev, args.n, args.form, args.slices, args.steps, args.warmup)
+            metric = "one contraction of the precision workload (profiling case)"
+        elif args.workload == "permute":
+            res = permute_case(dev, args.perm_e, args.steps, args.warmup)
+            metric = "permutation kernel GB/s (profiling case)"
         else:
             res = serve_bench(dev, [1000, 3000, 10000, 30000, 100000], args.serve_seconds)
             metric = "served contractions/s with p50/p99 ms (Poisson arrivals)"
@@ -419,17 +583,58 @@ def main():
     C = m.empty_colmajor([n, n], torch.complex128, dev)
     Cn = m.empty_colmajor([n, n], torch.complex128, dev)
     c_h = torch.empty_like(C, device="cpu").pin_memory()
-    plan = m.contraction_plan(A, [m.Index(x) for x in ia], B, [m.Index(x) for x in ib], C,
-                              [m.Index(x) for x in ic], "ozaki", args.slices)
-    pln = m.contraction_plan(A, [m.Index(x) for x in ia], B, [m.Index(x) for x in ib], Cn,
-                             [m.Index(x) for x in ic], "plain", 0)
-    ws_t = torch.empty(max(plan.workspace_bytes, 1), dtype=torch.uint8, device=dev)
+    labels = ([m.Index(x) for x in ia], [m.Index(x) for x in ib], [m.Index(x) for x in ic])
+
+    def oz_plan(S, out=C):
+        return m.contraction_plan(A, labels[0], B, labels[1], out, labels[2], "ozaki", S)
+
+    pln = m.contraction_plan(A, labels[0], B, labels[1], Cn, labels[2], "plain", 0)
+    sweep_s = (5, 6, 7, 8)
+    ws_t = torch.empty(max(max(oz_plan(S).workspace_bytes for S in sweep_s), 1), dtype=torch.uint8, device=dev)
     lib = _lib.load()
     stream = torch.cuda.current_stream(dev)
 
-    def step(p=plan, out=C):
+    def launch(p, out):
         _lib.check(lib.mgb_contract(p.handle, A.data_ptr(), B.data_ptr(), out.data_ptr(), ws_t.data_ptr(),
                                     ws_t.numel(), stream.cuda_stream), lib)
+
+    def rel(x, y):
+        return (torch.linalg.vector_norm((x - y).flatten()) / torch.linalg.vector_norm(y.flatten())).item()
+
+    # native FP64 (DMMA) on the same shapes: the FP64 reference for every error
+    launch(pln, Cn)  # warm-up
+    torch.cuda.synchronize()
+    en0, en1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    en0.record(stream)
+    for _ in range(args.native_steps):
+        launch(pln, Cn)
+    en1.record(stream)
+    torch.cuda.synchronize()
+    native_ms = en0.elapsed_time(en1) / args.native_steps
+
+    # slice count swept 5..8: time and error of each
+    sweep = []
+    for S in sweep_s:
+        p = oz_plan(S)
+        launch(p, C)
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(2):
+            launch(p, C)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        sms = t0.elapsed_time(t1) / 2
+        sweep.append({"slices": S, "ms": sms, "tflops": p.flops / (sms / 1e3) / 1e12, "rel_err": rel(C, Cn)})
+    if args.slices:
+        S = args.slices
+    else:
+        ok = [x for x in sweep if x["rel_err"] <= 1e-13]
+        S = min(ok, key=lambda x: x["ms"])["slices"] if ok else 8
+    plan = oz_plan(S)
+
+    def step(p=plan, out=C):
+        launch(p, out)
 
     for _ in range(args.warmup):
         step()
@@ -461,28 +666,45 @@ def main():
         mainv.append(fm.value)
     lib.mgb_plan_set_timing(plan.handle, 0)
     gemm_ms = statistics.mean(mainv)
-    S = args.slices
     pairs = S * (S + 1) // 2
     tensor_flops = 2.0 * pairs * n * (2 * n) * (2 * 8192)
     bf16_peak, hbm_peak, peak_kind = peaks()
     achieved = tensor_flops / (gemm_ms / 1e3) / 1e12
-    traffic = ncu_traffic()
+    traffic = ncu_traffic(S)
 
-    # native FP64 (DMMA) on the same shapes: the FP64 reference for the error
-    torch.cuda.synchronize()
-    en0, en1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    step(pln, Cn)  # warm-up
-    torch.cuda.synchronize()
-    en0.record(stream)
-    for _ in range(args.native_steps):
-        step(pln, Cn)
-    en1.record(stream)
-    torch.cuda.synchronize()
-    native_ms = en0.elapsed_time(en1) / args.native_steps
     native = flops / (native_ms / 1e3) / 1e12
     step()
     torch.cuda.synchronize()
-    rel_err = (torch.linalg.vector_norm((C - Cn).flatten()) / torch.linalg.vector_norm(Cn.flatten())).item()
+    rel_err = rel(C, Cn)
+
+    # Float32 variant (ComplexF32, BF16x3) on the same shapes; its FP64
+    # reference is the plain form on the same rounded inputs
+    A32, B32 = A.to(torch.complex64), B.to(torch.complex64)
+    C32 = m.empty_colmajor([n, n], torch.complex64, dev)
+    p32 = m.contraction_plan(A32, labels[0], B32, labels[1], C32, labels[2], "bf16x3", 0)
+    ws32 = torch.empty(max(p32.workspace_bytes, 1), dtype=torch.uint8, device=dev)
+
+    def run32():
+        _lib.check(lib.mgb_contract(p32.handle, A32.data_ptr(), B32.data_ptr(), C32.data_ptr(), ws32.data_ptr(),
+                                    ws32.numel(), stream.cuda_stream), lib)
+
+    run32()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        run32()
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms32 = f0.elapsed_time(f1) / args.steps
+    A.copy_(A32)
+    B.copy_(B32)
+    launch(pln, Cn)
+    torch.cuda.synchronize()
+    f32 = {"form": "bf16x3", "dtype": "c32", "ms_per_step": ms32, "value": p32.flops / (ms32 / 1e3) / 1e12,
+           "unit": "TFLOP/s", "rel_err": rel(C32.to(torch.complex128), Cn),
+           "rel_err_reference": "plain FP64 DMMA on the ComplexF32 inputs widened"}
+    del A32, B32, C32, ws32
 
     # end to end through the public API with host buffers
     def e2e_step():
@@ -517,8 +739,10 @@ def main():
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64", "data": "synthetic", "config": workload_config(n),
-            "form": f"ozaki S={S} (bf16 digits of 7 bits on tcgen05.mma kind::f16, exact int accumulation)",
+            "form": f"ozaki S={S} (bf16 digits of {8 if S <= 6 else 7} bits on tcgen05.mma kind::f16, exact int "
+                    "accumulation)",
             "rel_err": rel_err, "rel_err_reference": "plain FP64 DMMA result on the same inputs",
+            "slice_sweep": sweep, "float32_variant": f32,
             "native": {"value": native, "unit": "TFLOP/s", "ms_per_step": native_ms, "form": "plain FP64 DMMA (4M)"},
             "speedup_vs_native": value / native,
             "e2e": {"value": e2e, "unit": "TFLOP/s", "ms_per_step": e2e_ms / args.steps,

@@ -166,7 +166,7 @@ int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan) {
     if (!group || !tile_per_plan) return fail(MGB_ERR_ARGUMENT, "group: null argument");
     for (auto &b : group->buckets) {
         const int t = tile_per_plan[b.members.front()];
-        b.cp.band = (t >= 0 && t < 6) ? kBands[t] : 16;
+        b.cp.band = (t >= 0 && t < 6) ? kBands[t] : 0;
     }
     return MGB_OK;
 }

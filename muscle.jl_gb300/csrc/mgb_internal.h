@@ -99,7 +99,7 @@ struct ContractionPlan {
     // arrays of L pointers) replace the batch strides when set.
     const void *const *pa = nullptr, *const *pb = nullptr;
     void *const *pc = nullptr;
-    int band = 16;         // tensor-core kernel: row tiles per rasterisation band
+    int band = 0;          // tensor-core kernel: row tiles per rasterisation band (0: default)
     uint64_t ws_bytes = 0;
     // workspace layout (byte offsets)
     uint64_t ws_a = 0, ws_b = 0, ws_scale_a = 0, ws_scale_b = 0;

@@ -11,7 +11,7 @@
 //   Products s_i t_j with i + j = d share the scale 2^(-W d) and go to one
 //   TMEM accumulator per d ("group"); pairs with i + j > S + 1 are dropped
 //   (Ozaki scheme I).  Every KC embedded k (KC = 256 for W = 7, 128 for
-//   W = 8) the epilogue warps read each group's float32 partial sums (exact
+//   W = 8) the epilogue warps read every group's float32 partial sums (exact
 //   integers), convert them to int and add them, shifted left by
 //   W (S + 1 - d), into one exact 96-bit integer per output element
 //   (|X| < 2^(log2 K + W (S + 1) + 1) < 2^95 for any K below 2^31). The only
@@ -19,30 +19,30 @@
 //   element (GB300's FP64 pipe is slow).
 //   Group bound per k: max(d + 1, 4) * 2^(2W-2); KC * bound <= 2^24 for
 //   d <= 15 (W = 7) and d <= 7 (W = 8), which covers every group of every
-//   supported S (d <= S + 1).  The chunk boundaries of the groups are
-//   staggered by one k block each, so at most ceil(groups / chunk blocks)
-//   groups are being read out at any time; that many spare TMEM
-//   accumulators rotate through the groups and the MMA issuer never waits
-//   for a readout in the middle of a k block.
+//   supported S (d <= S + 1).
 //
 // BF16X3 (Float32 / ComplexF32 results)
 //   x = hi + mid + lo, three bf16 pieces (exact for normal floats); the six
-//   products with piece-index sum <= 4 are kept. The tensor core accumulates
-//   in float32 with truncation, whose bias grows with the number of
-//   accumulations, so hi*hi and the five smaller products go to two separate
-//   TMEM accumulators, double-buffered, read out every KC = 256 k and summed
-//   in registers with Kahan compensation.
+//   products with piece-index sum <= 2 (0-based) are kept. The tensor core
+//   accumulates in float32 with truncation, whose bias grows with the number
+//   of accumulations, so the products are grouped by piece-index sum like
+//   the digit groups (hi*hi alone, then sums 1 and 2), read out every
+//   KC = 256 k and summed in registers with Kahan compensation.
 //
 // Complex operands are embedded as real GEMMs: A_e[m][2k+p] = part_p(A[m,k]),
 // B_e[2n+q][2k+p] holds [[Br, -Bi], [Bi, Br]] so that C_e[m][2n+q] is part q
 // of C[m,n] (4 real products per complex product, as zgemm's 4M form).
 //
-// Pipeline per CTA (128 x 64 embedded outputs, one CTA per SM):
+// Pipeline per CTA (128 x 32 embedded outputs, one CTA per SM):
 //   warp 0       TMA producer: one 3-D box per operand per 32-wide k block
 //                loads all S slices at once into a 64B-swizzled stage;
-//   warp 1       TMEM allocation, then a single thread issues
-//                tcgen05.mma.cta_group::1.kind::f16 (M=128, N=64, K=16);
-//   warps 2..9   epilogue: tcgen05.ld 32x32b.x32 per group and column half.
+//   warp 1       TMEM allocation, then a single thread issues, per 16 k,
+//                one tcgen05.mma.cta_group::1.kind::f16 per A slice i with
+//                M = 128, N = 32 (S - i): B slices 0 .. S-1-i lie back to
+//                back in the stage and their accumulators (digit groups
+//                i .. S-1) lie back to back in TMEM;
+//   warps 2..9   epilogue: tcgen05.ld 32x32b.x16 per group and column half,
+//                from the bank the MMAs are not writing.
 // Every mbarrier wait is bounded; on timeout the CTA records
 // MGB_ERR_DEVICE_TIMEOUT in the device status word, drains its copies and
 // MMAs, frees TMEM and returns.
@@ -59,14 +59,15 @@ namespace mgb {
 
 constexpr int OZ_KC = 256;     // BF16X3: embedded k between readouts
 constexpr int OZ_BM = 128;     // rows of A per CTA (TMEM lanes)
-constexpr int OZ_BN = 64;      // embedded rows of B per CTA
+constexpr int OZ_BN = 32;      // embedded rows of B per CTA = TMEM columns of one digit group
 constexpr int OZ_BK = 32;      // k per stage (64-byte swizzled rows)
 constexpr int OZ_EPI_WARPS = 8;
-constexpr int OZ_GROUP_M = 16;  // row tiles per rasterisation band
+constexpr int OZ_GROUP_M = 8;  // row tiles per rasterisation band
 constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;
 constexpr int OZ_A_TILE = OZ_BM * OZ_BK * 2;  // 8192 bytes per slice
-constexpr int OZ_B_TILE = OZ_BN * OZ_BK * 2;  // 4096 bytes per slice
-constexpr int OZ_SMEM_BUDGET = 200 * 1024;
+constexpr int OZ_B_TILE = OZ_BN * OZ_BK * 2;  // 2048 bytes per slice
+constexpr int OZ_SMEM_BUDGET = 220 * 1024;
+constexpr int OZ_MAX_STAGES = 6;
 constexpr long long OZ_TIMEOUT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 __host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (OZ_A_TILE + OZ_B_TILE); }
@@ -78,13 +79,16 @@ __host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (OZ_A_TILE 
 __host__ __device__ constexpr int oz_digit_bits(int S) { return S <= 6 ? 8 : 7; }
 __host__ __device__ constexpr int oz_chunk_blocks(int S) { return oz_digit_bits(S) == 8 ? 4 : 8; }
 __host__ __device__ constexpr int oz_stages(int S) {
-    return (OZ_SMEM_BUDGET / oz_stage_bytes(S)) < 4 ? (OZ_SMEM_BUDGET / oz_stage_bytes(S)) : 4;
+    return (OZ_SMEM_BUDGET / oz_stage_bytes(S)) < OZ_MAX_STAGES ? (OZ_SMEM_BUDGET / oz_stage_bytes(S))
+                                                                : OZ_MAX_STAGES;
 }
-__host__ __device__ constexpr int oz_tmem_cols(int nacc) {
-    return nacc * OZ_BN <= 64 ? 64 : nacc * OZ_BN <= 128 ? 128 : nacc * OZ_BN <= 256 ? 256 : 512;
-}
+// two banks of S groups of OZ_BN columns, each bank rounded up to 128 or 256
+// columns (bank bases at column 0 and TCOLS / 2)
+__host__ __device__ constexpr int oz_tmem_cols(int S) { return S * OZ_BN <= 128 ? 256 : 512; }
+// More than half of the SM's shared memory for every S, so one CTA (and one
+// TMEM allocation) per SM.
 __host__ __device__ constexpr int oz_smem_bytes(int S) {
-    return oz_stages(S) * oz_stage_bytes(S) + 1024 /*align*/ + 512 /*barriers*/;
+    return oz_stages(S) * oz_stage_bytes(S) + 1024 /*align*/ + 256 /*barriers*/;
 }
 
 // =============================================================================
@@ -165,30 +169,13 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
-// Predicated MMA: issued only when `issue` != 0. Keeping the issuing thread's
-// instruction stream free of branches matters: a taken branch between two
-// tcgen05.mma instructions costs far more issue time than extra arithmetic.
-__device__ __forceinline__ void tc_mma_if(uint32_t issue, uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
-                                          uint32_t idesc, uint32_t accumulate) {
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile(
-        "{\n\t.reg .pred p, q;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "setp.ne.b32 q, %5, 0;\n\t"
-        "@q tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate), "r"(issue)
-        : "memory");
-}
-
-__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
           "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-          "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
-          "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
-          "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          "=r"(v[14]), "=r"(v[15])
         : "r"(taddr)
         : "memory");
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -209,10 +196,6 @@ __device__ __forceinline__ double x96_to_double(uint32_t w0, uint32_t w1, uint32
     return fma(__ll2double_rn(hi), 4294967296.0, __uint2double_rn(w0));
 }
 
-// Staggered exact chunks: digit group g closes a chunk after k block kb when
-// g == (kb + 1) % kcb, and every group closes its last chunk after the last
-// block. Each chunk spans at most kcb blocks (KC = kcb * 32 embedded k), so
-// the float32 partial sums stay exact; one group is read out per k block.
 // K-major operand tile, 64-byte swizzle: rows of 64 B, 8-row atoms of 512 B.
 __device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
     uint64_t d = 0;
@@ -223,10 +206,10 @@ __device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
     d |= (uint64_t)4 << 61;                   // swizzle mode: 64 B
     return d;
 }
-// kind::f16 instruction descriptor: f32 accumulate, bf16 A and B, both K-major.
-__host__ __device__ constexpr uint32_t oz_idesc() {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) |
-           ((uint32_t)(OZ_BM >> 4) << 24);
+// kind::f16 instruction descriptor: f32 accumulate, bf16 A and B, both
+// K-major, M = 128, N = n (a multiple of 16 up to 256).
+__host__ __device__ constexpr uint32_t oz_idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(OZ_BM >> 4) << 24);
 }
 
 // =============================================================================
@@ -478,7 +461,7 @@ __global__ void __launch_bounds__(256) k_oz_slice(const T *__restrict__ X, OpGeo
 struct OzGemmArgs {
     int64_t M, Ne, N;      // rows of A, embedded rows of B, un-embedded N
     int32_t nkb;           // number of 32-wide k blocks
-    int32_t kcb;           // k blocks per exact chunk
+    int32_t kcb;           // k blocks per chunk (exact readout interval)
     int32_t S;             // slices (digits / pieces)
     const int32_t *expA;   // [L][M] biased exponents (OZAKI)
     const int32_t *expB;   // [L][N]
@@ -489,44 +472,43 @@ struct OzGemmArgs {
     int32_t *status;
 };
 
+// One CTA computes a 128 x 32 tile of the embedded output. Digit group
+// g = i + j (0-based slice indices of A and B) owns 32 TMEM columns; the S
+// groups of a chunk form one bank of 32 S columns, and two banks alternate
+// so that the epilogue reads chunk c while the MMAs fill chunk c + 1.
+// The B slices of a stage lie back to back (32 rows each), so the products
+// of A slice i with B slices 0 .. S-1-i are ONE tcgen05.mma with
+// N = 32 (S - i) whose accumulator columns are exactly groups i .. S-1:
+// S wide MMAs per 16 k instead of S (S+1)/2 narrow ones, and every A slice
+// is read from shared memory once per 16 k.
 template <int S, bool EXACT, bool CX>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_oz_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const OzGemmArgs args) {
-    // NG accumulators (digit groups, or hi/lo for BF16X3) per buffer; BF16X3
-    // double-buffers them so the MMA never waits for the readout.
-    constexpr int NG = EXACT ? S : 2;
-    constexpr int NB = EXACT ? 1 : 2;
-    constexpr int W = oz_digit_bits(S);     // digit width (EXACT)
-    constexpr int KCB = oz_chunk_blocks(S); // exact chunk length in k blocks (EXACT)
-    // ROT: spare accumulator slots; a digit group whose chunk ends moves to a
-    // free slot and leaves the old one to the epilogue. Up to ceil(NG / KCB)
-    // groups end together, so that many spares are needed (S <= 7 fits TMEM).
-    constexpr int NSPARE = (NG + KCB - 1) / KCB;
-    constexpr bool ROT = EXACT && NG + NSPARE <= 8;
-    constexpr int NSLOT = ROT ? NG + NSPARE : NG * NB;
+    constexpr int W = oz_digit_bits(S);  // digit width (EXACT)
     constexpr int NST = oz_stages(S);
     constexpr int STAGE = oz_stage_bytes(S);
-    constexpr int TCOLS = oz_tmem_cols(NSLOT);
+    constexpr int TCOLS = oz_tmem_cols(S);
+    constexpr int BANK = TCOLS / 2;  // TMEM column offset of the second bank (128 or 256)
     static_assert(NST >= 2, "need at least two pipeline stages");
-    static_assert(NSLOT * OZ_BN <= 512, "TMEM holds at most 512 columns");
+    static_assert(OZ_BN * S <= BANK && TCOLS <= 512, "two banks must fit in TMEM");
+    static_assert(OZ_BN * S <= 256, "one MMA covers at most 256 columns");
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + NST * STAGE);
-    uint64_t *full = bars;              // [NST]
-    uint64_t *empty = bars + NST;       // [NST]
-    constexpr int NFULL = EXACT ? NG : NB;      // chunk-complete barriers
-    uint64_t *acc_full = bars + 2 * NST;        // [NFULL]
-    uint64_t *acc_empty = acc_full + NFULL;     // [NSLOT] (per physical accumulator)
-    uint64_t *done = acc_empty + NSLOT;
+    uint64_t *full = bars;               // [NST]
+    uint64_t *empty = bars + NST;        // [NST]
+    uint64_t *acc_full = bars + 2 * NST; // [2] bank filled (one commit)
+    uint64_t *acc_empty = acc_full + 2;  // [2] bank read (one arrive per epilogue warp)
+    uint64_t *done = acc_empty + 2;
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    // Grouped rasterisation: consecutive CTAs walk a band of OZ_GROUP_M row
-    // tiles across all column tiles, so the slices of A and B they read are
-    // shared in L2 by the CTAs resident at the same time.
+    // Grouped rasterisation: consecutive CTAs walk a band of `band` row tiles
+    // across all column tiles, so the slices of A and B they read are shared
+    // in L2 by the CTAs resident at the same time.
     int64_t m_tile, n_tile;
     {
         const int64_t nm = gridDim.y, nn = gridDim.x;
@@ -547,8 +529,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             mbar_init(smem_u32(full + s), 1);
             mbar_init(smem_u32(empty + s), 1);
         }
-        for (int b = 0; b < NFULL; ++b) mbar_init(smem_u32(acc_full + b), 1);
-        for (int g = 0; g < NSLOT; ++g) mbar_init(smem_u32(acc_empty + g), OZ_EPI_WARPS);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(acc_full + b), 1);
+            mbar_init(smem_u32(acc_empty + b), OZ_EPI_WARPS);
+        }
         mbar_init(smem_u32(done), 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -590,162 +574,38 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            const uint32_t idesc = oz_idesc();
             bool ok = true;
-            if constexpr (ROT) {
-                // Group g closes a chunk after k block kb when g % KCB == (kb + 1) % KCB.
-                // slot of group g: 4 bits of `map`; free slots: FIFO of 4-bit ids in fq
-                uint32_t map = 0, fq = 0, fill = 0;  // fill bit x: parity of chunks left in slot x
-#pragma unroll
-                for (int g = 0; g < NG; ++g) map |= (uint32_t)g << (4 * g);
-#pragma unroll
-                for (int x = NG; x < NSLOT; ++x) fq |= (uint32_t)x << (4 * (x - NG));
-                for (int kb = 0; kb < nkb && ok; ++kb) {
-                    const int s = kb % NST;
-                    const uint32_t round = kb / NST;
-                    if (!mbar_wait(smem_u32(full + s), round & 1, abort_flag, args.status)) {
-                        ok = false;
-                        break;
-                    }
-                    const int r = kb % KCB;  // groups g % KCB == r start a new chunk (kb > 0)
-                    if (kb > 0) {
-                        for (int g = r; g < NG && ok; g += KCB) {
-                            const uint32_t nw = fq & 15u;
-                            const uint32_t old = (map >> (4 * g)) & 15u;
-                            fq = (fq >> 4) | (old << (4 * (NSPARE - 1)));
-                            map = (map & ~(15u << (4 * g))) | (nw << (4 * g));
-                            // the chunk previously left in slot nw must have been read out
-                            ok = mbar_wait(smem_u32(acc_empty + nw), ((fill >> nw) & 1u) ^ 1u, abort_flag,
-                                           args.status);
-                        }
-                        if (!ok) break;
-                    }
-                    tc_fence_after();
-                    const uint32_t a_base = smem_u32(smem + s * STAGE);
-                    const uint64_t ad0 = sw64_desc(a_base);
-                    const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
-#pragma unroll
-                    for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
-#pragma unroll
-                        for (int i = 0; i < S; ++i)
-#pragma unroll
-                            for (int j = 0; j < S - i; ++j) {
-                                const int g = i + j;
-                                const uint32_t d = tmem + ((map >> (4 * g)) & 15u) * OZ_BN;
-                                const uint32_t acc = (k16 == 0 && i == 0 && (kb == 0 || g % KCB == r)) ? 0u : 1u;
-                                tc_mma_if(1u, d, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
-                                          bd0 + (uint64_t)((j * OZ_B_TILE + k16 * 32) >> 4), idesc, acc);
-                            }
-                    tc_commit(smem_u32(empty + s));
-                    if (kb == nkb - 1) {
-                        for (int g = 0; g < NG; ++g) tc_commit(smem_u32(acc_full + g));
-                    } else {
-                        for (int g = (kb + 1) % KCB; g < NG; g += KCB) {  // groups whose chunk ends here
-                            tc_commit(smem_u32(acc_full + g));
-                            fill ^= 1u << ((map >> (4 * g)) & 15u);
-                        }
-                    }
+            for (int kb = 0; kb < nkb && ok; ++kb) {
+                const int s = kb % NST;
+                const int c = kb / kcb;          // chunk
+                const int kin = kb - c * kcb;    // k block inside the chunk
+                const uint32_t bank = (uint32_t)c & 1u;
+                if (!mbar_wait(smem_u32(full + s), (kb / NST) & 1, abort_flag, args.status)) {
+                    ok = false;
+                    break;
                 }
-            } else if constexpr (EXACT) {
-                // Group g closes its chunks at k blocks kb with (kb + 1 - g) % kcb == 0
-                // (staggered), so one group is read out per k block; the group that
-                // starts a chunk gets its MMAs last, after the other groups' work.
-                uint32_t par = 0;  // bit g: parity of group g's completed chunks
-                for (int kb = 0; kb < nkb && ok; ++kb) {
-                    const int s = kb % NST;
-                    const uint32_t round = kb / NST;
-                    if (!mbar_wait(smem_u32(full + s), round & 1, abort_flag, args.status)) {
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-                    const uint32_t a_base = smem_u32(smem + s * STAGE);
-                    const uint64_t ad0 = sw64_desc(a_base);
-                    const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
-                    // group starting a chunk in this k block (-1: block 0, where all start)
-                    const int gs = kb == 0 ? -1 : kb % kcb;
-                    const uint32_t not_first = kb == 0 ? 0u : 1u;
-                    // pass 1: every group except gs, i-major so that consecutive MMAs
-                    // go to different accumulators; fully unrolled and predicated
-#pragma unroll
-                    for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
-#pragma unroll
-                        for (int i = 0; i < S; ++i)
-#pragma unroll
-                            for (int j = 0; j < S - i; ++j) {
-                                const int g = i + j;
-                                const uint32_t acc = (k16 == 0 && i == 0) ? not_first : 1u;
-                                tc_mma_if(g != gs, tmem + g * OZ_BN, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
-                                          bd0 + (uint64_t)((j * OZ_B_TILE + k16 * 32) >> 4), idesc, acc);
-                            }
-                    // pass 2: group gs, once the epilogue has read its previous chunk
-                    if (gs >= 0 && gs < NG) {
-                        ok = mbar_wait(smem_u32(acc_empty + gs), ((par >> gs) & 1) ^ 1, abort_flag, args.status);
-                        if (!ok) break;
-                        tc_fence_after();
-                        const uint32_t dg = tmem + gs * OZ_BN;
-#pragma unroll
-                        for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
-#pragma unroll
-                            for (int i = 0; i < S; ++i) {
-                                const int j = gs - i;  // >= 0 exactly when i <= gs
-                                tc_mma_if(i <= gs, dg, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
-                                          bd0 + (uint64_t)((max(j, 0) * OZ_B_TILE + k16 * 32) >> 4), idesc,
-                                          (k16 == 0 && i == 0) ? 0u : 1u);
-                            }
-                    }
-                    tc_commit(smem_u32(empty + s));
-                    if (kb == nkb - 1) {
-                        for (int g = 0; g < NG; ++g) tc_commit(smem_u32(acc_full + g));
-                    } else if ((kb + 1) % kcb < NG) {
-                        const int g = (kb + 1) % kcb;
-                        tc_commit(smem_u32(acc_full + g));
-                        par ^= 1u << g;
-                    }
+                // a chunk starts in a bank once the epilogue has read the chunk
+                // two before it (the wait passes at once for the first two)
+                if (kin == 0 &&
+                    !mbar_wait(smem_u32(acc_empty + bank), ((uint32_t)(c >> 1) & 1u) ^ 1u, abort_flag, args.status)) {
+                    ok = false;
+                    break;
                 }
-            } else {
-                int chunk = 0;
-                for (int kb = 0; kb < nkb && ok; ++kb) {
-                    const int s = kb % NST;
-                    const uint32_t round = kb / NST;
-                    const bool chunk_start = (kb % kcb) == 0;
-                    const int buf = chunk % NB;       // accumulator buffer of this chunk
-                    const uint32_t use = chunk / NB;  // earlier uses of that buffer
-                    if (!mbar_wait(smem_u32(full + s), round & 1, abort_flag, args.status)) {
-                        ok = false;
-                        break;
-                    }
-                    if (chunk_start) {
-                        // both accumulators of this buffer must have been read out
-                        ok = mbar_wait(smem_u32(acc_empty + buf * NG + 0), (use & 1) ^ 1, abort_flag, args.status) &&
-                             mbar_wait(smem_u32(acc_empty + buf * NG + 1), (use & 1) ^ 1, abort_flag, args.status);
-                        if (!ok) break;
-                    }
-                    tc_fence_after();
-                    const uint32_t a_base = smem_u32(smem + s * STAGE);
-                    const uint64_t ad0 = sw64_desc(a_base);
-                    const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
-                    const uint32_t t_hi = tmem + (buf * NG + 0) * OZ_BN, t_lo = tmem + (buf * NG + 1) * OZ_BN;
-                    const uint32_t not_first = chunk_start ? 0u : 1u;
+                tc_fence_after();
+                const uint32_t a_base = smem_u32(smem + s * STAGE);
+                const uint64_t ad0 = sw64_desc(a_base);
+                const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
+                const uint32_t d0 = tmem + bank * BANK;
+                const uint32_t first = kin == 0 ? 0u : 1u;
 #pragma unroll
-                    for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
+                for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
 #pragma unroll
-                        for (int i = 0; i < S; ++i)
-#pragma unroll
-                            for (int j = 0; j < S - i; ++j) {
-                                // hi*hi apart from the five smaller products
-                                const bool hi = (i | j) == 0;
-                                const bool lo_first = i == 0 && j == 1;  // first product into t_lo
-                                const uint32_t acc = (k16 == 0 && (hi || lo_first)) ? not_first : 1u;
-                                tc_mma_if(1u, hi ? t_hi : t_lo, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
-                                          bd0 + (uint64_t)((j * OZ_B_TILE + k16 * 32) >> 4), idesc, acc);
-                            }
-                    tc_commit(smem_u32(empty + s));
-                    if ((kb % kcb) == kcb - 1 || kb == nkb - 1) {
-                        tc_commit(smem_u32(acc_full + buf));
-                        ++chunk;
-                    }
-                }
+                    for (int i = 0; i < S; ++i)
+                        tc_mma(d0 + OZ_BN * i, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
+                               bd0 + (uint64_t)((k16 * 32) >> 4), oz_idesc(OZ_BN * (S - i)),
+                               (k16 == 0 && i == 0) ? first : 1u);
+                tc_commit(smem_u32(empty + s));
+                if (kin == kcb - 1 || kb == nkb - 1) tc_commit(smem_u32(acc_full + bank));
             }
             // wait for every MMA this thread issued before TMEM is released
             tc_commit(smem_u32(done));
@@ -753,17 +613,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         }
     } else {
         // ---------------- epilogue ----------------
-        const int q = warp % 4;           // TMEM lane quarter this warp may access
-        const int h = (warp - 2) / 4;     // column half of each group
+        const int q = warp % 4;        // TMEM lane quarter this warp may access
+        const int h = (warp - 2) / 4;  // column half (16 columns) of each group
         const int64_t row = m0 + 32 * q + lane;
-        const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + 32 * h;
+        const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + 16 * h;
         // EXACT: one 96-bit two's-complement integer per output column,
         // X = sum_d G_d 2^(W (S + 1 - d)), held in w0 (bits 0-31), w1, w2.
-        uint32_t w0[EXACT ? 32 : 1], w1[EXACT ? 32 : 1], w2[EXACT ? 32 : 1];
+        uint32_t w0[EXACT ? 16 : 1], w1[EXACT ? 16 : 1], w2[EXACT ? 16 : 1];
         // BF16X3: Kahan-compensated float32 sum over the chunks
-        float accf[EXACT ? 1 : 32], comp[EXACT ? 1 : 32];
+        float accf[EXACT ? 1 : 16], comp[EXACT ? 1 : 16];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
+        for (int j = 0; j < 16; ++j) {
             if (EXACT) {
                 w0[j] = 0;
                 w1[j] = 0;
@@ -774,123 +634,53 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             }
         }
         bool ok = true;
-        if constexpr (ROT) {
-            // Readout events in order: after k block kb < nkb - 1 the groups with
-            // g % KCB == (kb + 1) % KCB close a chunk; after the last block every
-            // group closes its last one. Slots follow the MMA side's map and queue.
-            uint32_t map = 0, fq = 0, par = 0;
-#pragma unroll
-            for (int g = 0; g < NG; ++g) map |= (uint32_t)g << (4 * g);
-#pragma unroll
-            for (int x = NG; x < NSLOT; ++x) fq |= (uint32_t)x << (4 * (x - NG));
-            int kb = 0, g = (nkb > 1) ? 1 % KCB : 0;
-            bool last = nkb == 1;
-            while (ok) {
-                // next event (kb, g): skip block boundaries without a closing group
-                if (!last) {
-                    while (g >= NG) {
-                        ++kb;
-                        if (kb == nkb - 1) {
-                            last = true;
-                            g = 0;
-                            break;
-                        }
-                        g = (kb + 1) % KCB;
-                    }
-                }
-                if (last && g >= NG) break;
-                const uint32_t x = (map >> (4 * g)) & 15u;
-                if (!mbar_wait(smem_u32(acc_full + g), (par >> g) & 1, abort_flag, args.status)) {
-                    ok = false;
-                    break;
-                }
-                par ^= 1u << g;
-                tc_fence_after();
-                uint32_t v[32];
-                tc_ld32(tbase + x * OZ_BN, v);
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(acc_empty + x));
-                if (!last) {  // group g continues in the oldest free slot
-                    const uint32_t nw = fq & 15u;
-                    fq = (fq >> 4) | (x << (4 * (NSPARE - 1)));
-                    map = (map & ~(15u << (4 * g))) | (nw << (4 * g));
-                }
-                const int sh = W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
-                if (sh < 32) {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
-                        add96(w0[j], w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32),
-                              t < 0 ? 0xFFFFFFFFu : 0u);
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
-                        add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
-                    }
-                }
-                g += last ? 1 : KCB;
-            }
-        } else if constexpr (EXACT) {
-            // Readout events in order: after k block kb < nkb - 1 group
-            // (kb + 1) % kcb (when it exists) closes a chunk; after the last
-            // block every group closes its last chunk.
-            uint32_t par = 0;  // bit g: parity of group g's chunks read so far
-            const int nev = nkb - 1 + NG;
 #pragma unroll 1
-            for (int e = 0; e < nev; ++e) {
-                const int g = e < nkb - 1 ? (e + 1) % kcb : e - (nkb - 1);
-                if (g >= NG) continue;
-                if (!mbar_wait(smem_u32(acc_full + g), (par >> g) & 1, abort_flag, args.status)) {
-                    ok = false;
-                    break;
-                }
-                par ^= 1u << g;
-                tc_fence_after();
-                uint32_t v[32];
-                tc_ld32(tbase + g * OZ_BN, v);
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(acc_empty + g));
-                const int sh = W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
-                if (sh < 32) {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
-                        add96(w0[j], w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32),
-                              t < 0 ? 0xFFFFFFFFu : 0u);
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
-                        add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
-                    }
-                }
+        for (int c = 0; c < nchunks; ++c) {
+            const uint32_t bank = (uint32_t)c & 1u;
+            if (!mbar_wait(smem_u32(acc_full + bank), (uint32_t)(c >> 1) & 1u, abort_flag, args.status)) {
+                ok = false;
+                break;
             }
-        } else {
-            for (int c = 0; c < nchunks && ok; ++c) {
-                const int buf = c % NB;
-                if (!mbar_wait(smem_u32(acc_full + buf), (c / NB) & 1, abort_flag, args.status)) {
-                    ok = false;
-                    break;
+            tc_fence_after();
+            const uint32_t tb = tbase + bank * BANK;
+            if constexpr (EXACT) {
+#pragma unroll
+                for (int g = 0; g < S; ++g) {
+                    uint32_t v[16];
+                    tc_ld16(tb + OZ_BN * g, v);
+                    if (g == S - 1) {  // every group of the bank is in registers
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));
+                    }
+                    const int sh = W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
+                    if (sh < 32) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
+                            add96(w0[j], w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32),
+                                  t < 0 ? 0xFFFFFFFFu : 0u);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
+                            add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
+                        }
+                    }
                 }
-                tc_fence_after();
-                // hi*hi and the smaller products of this chunk, then one compensated add
-                uint32_t vh[32], vl[32];
-                tc_ld32(tbase + (buf * NG + 0) * OZ_BN, vh);
-                tc_ld32(tbase + (buf * NG + 1) * OZ_BN, vl);
+            } else {
+                // pieces hi*hi, then the products of piece-index sum 1 and 2
+                uint32_t v0[16], v1[16], v2[16];
+                tc_ld16(tb, v0);
+                tc_ld16(tb + OZ_BN, v1);
+                tc_ld16(tb + 2 * OZ_BN, v2);
                 tc_fence_before();
                 __syncwarp();
-                if (lane == 0) {
-                    mbar_arrive(smem_u32(acc_empty + buf * NG + 0));
-                    mbar_arrive(smem_u32(acc_empty + buf * NG + 1));
-                }
+                if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    float x = __uint_as_float(vh[j]) + __uint_as_float(vl[j]);
+                for (int j = 0; j < 16; ++j) {
+                    float x = __uint_as_float(v0[j]) + (__uint_as_float(v1[j]) + __uint_as_float(v2[j]));
                     float y = x - comp[j];
                     float t = accf[j] + y;
                     comp[j] = (t - accf[j]) - y;
@@ -910,8 +700,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 erow = be == 0 ? -1022 : be - 1022;
             }
 #pragma unroll
-            for (int j = 0; j < 32; j += (CX ? 2 : 1)) {
-                int64_t ne = n0 + 32 * h + j;
+            for (int j = 0; j < 16; j += (CX ? 2 : 1)) {
+                int64_t ne = n0 + 16 * h + j;
                 if (ne >= args.Ne) continue;
                 int64_t n = CX ? (ne >> 1) : ne;
                 int64_t off = lb + om + group_offset(args.gn, 2, n);

@@ -25,10 +25,11 @@ pinned against every known-answer assertion of the reference's own tests for
 this path (tests/golden/kat_cases.json, generated by tests/golden/make_kat.py);
 bit-level parity with Julia's BLAS is unpinned (and not expected: BLAS
 summation order is unspecified). Floating-point parity is asserted at the
-spec tolerances (1e-13 / 1e-5 relative Frobenius).
+stated tolerances (1e-13 / 1e-5 relative Frobenius).
 """
 from __future__ import annotations
 
+import math
 from fractions import Fraction
 
 import numpy as np
@@ -203,6 +204,55 @@ def exact_entries(a, ia, b, ib, ic, positions):
             re += ar * br - ai * bi
             im += ar * bi + ai * br
         out.append(complex(float(re), float(im)) if cx else float(re))
+    return out
+
+
+def _veltkamp(x):
+    """x = hi + lo with hi, lo of at most 26 significant bits each, so that
+    every product of two halves is exact in float64 (Dekker 1971)."""
+    c = 134217729.0 * x  # 2^27 + 1
+    hi = c - (c - x)
+    return hi, x - hi
+
+
+def _exact_products(x, y):
+    xh, xl = _veltkamp(np.ascontiguousarray(x, dtype=np.float64).ravel())
+    yh, yl = _veltkamp(np.ascontiguousarray(y, dtype=np.float64).ravel())
+    return [xh * yh, xh * yl, xl * yh, xl * yl]
+
+
+def exact_dot(x, y):
+    """Correctly rounded sum_k x_k y_k of two float64 or complex128 vectors:
+    every product is split into exact float64 parts (Veltkamp/Dekker) and the
+    parts are summed with math.fsum (Shewchuk's exact summation)."""
+    x = np.asarray(x)
+    y = np.asarray(y)
+    if not (np.iscomplexobj(x) or np.iscomplexobj(y)):
+        return math.fsum(np.concatenate(_exact_products(x, y)))
+    xr, xi, yr, yi = x.real, x.imag, y.real, y.imag
+    re = np.concatenate(_exact_products(xr, yr) + _exact_products(-xi, yi))
+    im = np.concatenate(_exact_products(xr, yi) + _exact_products(xi, yr))
+    return complex(math.fsum(re), math.fsum(im))
+
+
+def exact_entries_fast(a, ia, b, ib, ic, positions):
+    """Correctly rounded values of selected entries of C = contract(a, b),
+    for checking results (and the FP64 oracle itself) at full problem sizes.
+    The contracted set follows the same rule as ``contract``: labels of both
+    operands that are not in ``ic``. positions: list of index tuples of C."""
+    ia, ib, ic = list(ia), list(ib), list(ic)
+    contr = [i for i in ia if i in ib and i not in ic]
+    out = []
+    for pos in positions:
+        fixed = dict(zip(ic, pos))
+
+        def vec(x, ix):
+            sel = tuple(fixed[i] if i in fixed else slice(None) for i in ix)
+            rest = [i for i in ix if i not in fixed]
+            sub = x[sel]
+            return np.transpose(sub, [rest.index(i) for i in contr]).ravel(order="F")
+
+        out.append(exact_dot(vec(a, ia), vec(b, ib)))
     return out
 
 

@@ -72,6 +72,27 @@ def test_contract_matches_exact_rational():
         assert abs(c[p] - e) <= 1e-14 * max(1.0, abs(e))
 
 
+def test_exact_dot_matches_rational():
+    """The fast exact entries (Veltkamp split + fsum) equal the rational
+    ones bit for bit, also over a 2^-20..2^20 magnitude spread."""
+    rng = np.random.default_rng(8)
+    a = wl.loguniform_complex(rng, (6, 40, 7))
+    b = wl.loguniform_complex(rng, (7, 5, 40))
+    ia, ib, ic = ["i", "k1", "k2"], ["k2", "j", "k1"], ["j", "i"]
+    pos = [(0, 0), (4, 5), (2, 3)]
+    assert ref.exact_entries_fast(a, ia, b, ib, ic, pos) == ref.exact_entries(a, ia, b, ib, ic, pos)
+    x = rng.standard_normal(300) * np.exp2(rng.uniform(-20, 20, 300))
+    y = rng.standard_normal(300)
+    assert ref.exact_dot(x, y) == ref.exact_entries(x, ["k"], y, ["k"], [], [()])[0]
+    # batch labels stay fixed
+    ab = rng.standard_normal((6, 7, 2))
+    bb = rng.standard_normal((7, 6, 2))
+    p2 = [(1, 2, 0), (5, 0, 1)]
+    lab = (["i", "k", "b"], ["k", "j", "b"], ["i", "j", "b"])
+    assert ref.exact_entries_fast(ab, lab[0], bb, lab[1], lab[2], p2) == ref.exact_entries(
+        ab, lab[0], bb, lab[1], lab[2], p2)
+
+
 def test_front_end_defaults():
     assert ref.front_inds_c(["i", "j"], ["j", "k"]) == ["i", "k"]
     assert ref.front_inds_c(["i", "j", "b"], ["j", "k", "b"], dims=["j"]) == ["i", "b", "k"]
