@@ -59,18 +59,20 @@ namespace mgb {
 
 constexpr int OZ_KC = 256;     // BF16X3: embedded k between readouts
 constexpr int OZ_BM = 128;     // rows of A per CTA (TMEM lanes)
-constexpr int OZ_BN = 32;      // embedded rows of B per CTA = TMEM columns of one digit group
 constexpr int OZ_BK = 32;      // k per stage (64-byte swizzled rows)
 constexpr int OZ_EPI_WARPS = 8;
 constexpr int OZ_GROUP_M = 8;  // row tiles per rasterisation band
 constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;
 constexpr int OZ_A_TILE = OZ_BM * OZ_BK * 2;  // 8192 bytes per slice
-constexpr int OZ_B_TILE = OZ_BN * OZ_BK * 2;  // 2048 bytes per slice
 constexpr int OZ_SMEM_BUDGET = 220 * 1024;
 constexpr int OZ_MAX_STAGES = 6;
 constexpr long long OZ_TIMEOUT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
-__host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (OZ_A_TILE + OZ_B_TILE); }
+// Columns per digit group (= embedded rows of B per CTA): two banks of S
+// groups must fit the 512 TMEM columns, and one MMA covers at most 256.
+__host__ __device__ constexpr int oz_bn(int S) { return S <= 3 ? 64 : 32; }
+__host__ __device__ constexpr int oz_b_tile(int S) { return oz_bn(S) * OZ_BK * 2; }  // bytes per slice
+__host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (OZ_A_TILE + oz_b_tile(S)); }
 // Digit width and exact chunk length (in 32-wide k blocks) per slice count.
 // W = 8 for S <= 6: |s1| <= 256, |si| <= 128, group bound max(d+1,4) 2^14, so a
 // float32 accumulator stays exact over 4 blocks (128 k) for every d <= 7.
@@ -82,9 +84,8 @@ __host__ __device__ constexpr int oz_stages(int S) {
     return (OZ_SMEM_BUDGET / oz_stage_bytes(S)) < OZ_MAX_STAGES ? (OZ_SMEM_BUDGET / oz_stage_bytes(S))
                                                                 : OZ_MAX_STAGES;
 }
-// two banks of S groups of OZ_BN columns, each bank rounded up to 128 or 256
-// columns (bank bases at column 0 and TCOLS / 2)
-__host__ __device__ constexpr int oz_tmem_cols(int S) { return S * OZ_BN <= 128 ? 256 : 512; }
+// two banks of S groups of oz_bn(S) columns; bank bases at columns 0 and 256
+__host__ __device__ constexpr int oz_tmem_cols(int) { return 512; }
 // More than half of the SM's shared memory for every S, so one CTA (and one
 // TMEM allocation) per SM.
 __host__ __device__ constexpr int oz_smem_bytes(int S) {
@@ -169,7 +170,8 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+// tcgen05.ld of 16 consecutive columns of this warp's 32 lanes (no wait)
+__device__ __forceinline__ void tc_ld16_issue(uint32_t taddr, uint32_t *v) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -178,6 +180,12 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
           "=r"(v[14]), "=r"(v[15])
         : "r"(taddr)
         : "memory");
+}
+// NC consecutive columns (a multiple of 16), then wait for the loads
+template <int NC>
+__device__ __forceinline__ void tc_ld(uint32_t taddr, uint32_t (&v)[NC]) {
+#pragma unroll
+    for (int c = 0; c < NC; c += 16) tc_ld16_issue(taddr + c, v + c);
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
@@ -472,15 +480,17 @@ struct OzGemmArgs {
     int32_t *status;
 };
 
-// One CTA computes a 128 x 32 tile of the embedded output. Digit group
-// g = i + j (0-based slice indices of A and B) owns 32 TMEM columns; the S
-// groups of a chunk form one bank of 32 S columns, and two banks alternate
+// One CTA computes a 128 x BN tile of the embedded output. Digit group
+// g = i + j (0-based slice indices of A and B) owns BN TMEM columns; the S
+// groups of a chunk form one bank of BN S columns, and two banks alternate
 // so that the epilogue reads chunk c while the MMAs fill chunk c + 1.
-// The B slices of a stage lie back to back (32 rows each), so the products
+// The B slices of a stage lie back to back (BN rows each), so the products
 // of A slice i with B slices 0 .. S-1-i are ONE tcgen05.mma with
-// N = 32 (S - i) whose accumulator columns are exactly groups i .. S-1:
+// N = BN (S - i) whose accumulator columns are exactly groups i .. S-1:
 // S wide MMAs per 16 k instead of S (S+1)/2 narrow ones, and every A slice
-// is read from shared memory once per 16 k.
+// is read from shared memory once per 16 k. BN = 64 for S = 3 (BF16X3
+// included) and 32 for S >= 4: the widest that two banks leave room for
+// while the epilogue's 96-bit accumulators stay in registers.
 template <int S, bool EXACT, bool CX>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_oz_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -488,11 +498,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     constexpr int W = oz_digit_bits(S);  // digit width (EXACT)
     constexpr int NST = oz_stages(S);
     constexpr int STAGE = oz_stage_bytes(S);
+    constexpr int BN = oz_bn(S);     // columns per digit group, embedded B rows per CTA
+    constexpr int HALF = BN / 2;     // columns per group read by one epilogue warp
     constexpr int TCOLS = oz_tmem_cols(S);
-    constexpr int BANK = TCOLS / 2;  // TMEM column offset of the second bank (128 or 256)
+    constexpr int BANK = TCOLS / 2;  // TMEM column offset of the second bank
     static_assert(NST >= 2, "need at least two pipeline stages");
-    static_assert(OZ_BN * S <= BANK && TCOLS <= 512, "two banks must fit in TMEM");
-    static_assert(OZ_BN * S <= 256, "one MMA covers at most 256 columns");
+    static_assert(BN * S <= BANK && TCOLS <= 512, "two banks must fit in TMEM");
+    static_assert(BN * S <= 256, "one MMA covers at most 256 columns");
+    static_assert(HALF % 16 == 0, "epilogue reads 16 columns at a time");
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -521,7 +534,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         m_tile = first + r % rows;
         n_tile = r / rows;
     }
-    const int64_t n0 = n_tile * OZ_BN, m0 = m_tile * OZ_BM;
+    const int64_t n0 = n_tile * BN, m0 = m_tile * OZ_BM;
     const int l = blockIdx.z;
 
     if (tid == 0) {
@@ -601,8 +614,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
 #pragma unroll
                     for (int i = 0; i < S; ++i)
-                        tc_mma(d0 + OZ_BN * i, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
-                               bd0 + (uint64_t)((k16 * 32) >> 4), oz_idesc(OZ_BN * (S - i)),
+                        tc_mma(d0 + BN * i, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
+                               bd0 + (uint64_t)((k16 * 32) >> 4), oz_idesc(BN * (S - i)),
                                (k16 == 0 && i == 0) ? first : 1u);
                 tc_commit(smem_u32(empty + s));
                 if (kin == kcb - 1 || kb == nkb - 1) tc_commit(smem_u32(acc_full + bank));
@@ -614,16 +627,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     } else {
         // ---------------- epilogue ----------------
         const int q = warp % 4;        // TMEM lane quarter this warp may access
-        const int h = (warp - 2) / 4;  // column half (16 columns) of each group
+        const int h = (warp - 2) / 4;  // column half (HALF columns) of each group
         const int64_t row = m0 + 32 * q + lane;
-        const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + 16 * h;
+        const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + HALF * h;
         // EXACT: one 96-bit two's-complement integer per output column,
         // X = sum_d G_d 2^(W (S + 1 - d)), held in w0 (bits 0-31), w1, w2.
-        uint32_t w0[EXACT ? 16 : 1], w1[EXACT ? 16 : 1], w2[EXACT ? 16 : 1];
+        uint32_t w0[EXACT ? HALF : 1], w1[EXACT ? HALF : 1], w2[EXACT ? HALF : 1];
         // BF16X3: Kahan-compensated float32 sum over the chunks
-        float accf[EXACT ? 1 : 16], comp[EXACT ? 1 : 16];
+        float accf[EXACT ? 1 : HALF], comp[EXACT ? 1 : HALF];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
+        for (int j = 0; j < HALF; ++j) {
             if (EXACT) {
                 w0[j] = 0;
                 w1[j] = 0;
@@ -646,8 +659,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             if constexpr (EXACT) {
 #pragma unroll
                 for (int g = 0; g < S; ++g) {
-                    uint32_t v[16];
-                    tc_ld16(tb + OZ_BN * g, v);
+                    uint32_t v[HALF];
+                    tc_ld<HALF>(tb + BN * g, v);
                     if (g == S - 1) {  // every group of the bank is in registers
                         tc_fence_before();
                         __syncwarp();
@@ -656,14 +669,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     const int sh = W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
                     if (sh < 32) {
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) {
+                        for (int j = 0; j < HALF; ++j) {
                             int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
                             add96(w0[j], w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32),
                                   t < 0 ? 0xFFFFFFFFu : 0u);
                         }
                     } else {
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) {
+                        for (int j = 0; j < HALF; ++j) {
                             int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
                             add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
                         }
@@ -671,15 +684,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 }
             } else {
                 // pieces hi*hi, then the products of piece-index sum 1 and 2
-                uint32_t v0[16], v1[16], v2[16];
-                tc_ld16(tb, v0);
-                tc_ld16(tb + OZ_BN, v1);
-                tc_ld16(tb + 2 * OZ_BN, v2);
+                uint32_t v0[HALF], v1[HALF], v2[HALF];
+                tc_ld<HALF>(tb, v0);
+                tc_ld<HALF>(tb + BN, v1);
+                tc_ld<HALF>(tb + 2 * BN, v2);
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
+                for (int j = 0; j < HALF; ++j) {
                     float x = __uint_as_float(v0[j]) + (__uint_as_float(v1[j]) + __uint_as_float(v2[j]));
                     float y = x - comp[j];
                     float t = accf[j] + y;
@@ -700,8 +713,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 erow = be == 0 ? -1022 : be - 1022;
             }
 #pragma unroll
-            for (int j = 0; j < 16; j += (CX ? 2 : 1)) {
-                int64_t ne = n0 + 16 * h + j;
+            for (int j = 0; j < HALF; j += (CX ? 2 : 1)) {
+                int64_t ne = n0 + HALF * h + j;
                 if (ne >= args.Ne) continue;
                 int64_t n = CX ? (ne >> 1) : ne;
                 int64_t off = lb + om + group_offset(args.gn, 2, n);
@@ -917,7 +930,8 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
     if (mid) MGB_CUDA_CHECK(cudaEventRecord(mid, s));
     CUtensorMap ta, tb;
     if ((st = make_map(&ta, sa, p.k_e, p.m_e, p.L * S, p.kpad, OZ_BM, S))) return st;
-    if ((st = make_map(&tb, sb, p.k_e, p.n_e, p.L * S, p.kpad, OZ_BN, S))) return st;
+    const int bn = oz_bn(S);
+    if ((st = make_map(&tb, sb, p.k_e, p.n_e, p.L * S, p.kpad, bn, S))) return st;
     OzGemmArgs a;
     a.M = p.M;
     a.Ne = p.n_e;
@@ -936,7 +950,7 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
     a.status = status;
     if (a.gm.n == 0) { a.gm.n = 1; a.gm.ext[0] = 1; for (int t = 0; t < 3; ++t) a.gm.str[t][0] = 0; }
     if (a.gn.n == 0) { a.gn.n = 1; a.gn.ext[0] = 1; for (int t = 0; t < 3; ++t) a.gn.str[t][0] = 0; }
-    dim3 grid((unsigned)((p.n_e + OZ_BN - 1) / OZ_BN), (unsigned)((p.M + OZ_BM - 1) / OZ_BM),
+    dim3 grid((unsigned)((p.n_e + bn - 1) / bn), (unsigned)((p.M + OZ_BM - 1) / OZ_BM),
               (unsigned)p.L);
     if ((p.M + OZ_BM - 1) / OZ_BM > 65535) return fail(MGB_ERR_UNSUPPORTED, "M too large for the grid");
     return launch_gemm(S, exact, cx, ta, tb, a, grid, s);

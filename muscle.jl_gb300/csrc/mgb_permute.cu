@@ -4,8 +4,8 @@
 // After folding, the copy is one of:
 //  * row copy   — the fastest mode of Y is also unit-stride in X: contiguous
 //                 rows, copied with 128-bit vectors when aligned;
-//  * transpose  — X and Y have different unit-stride modes: 32x32 (or 64x64
-//                 for 4-byte types) shared-memory tiles, coalesced on both
+//  * transpose  — X and Y have different unit-stride modes: 64x64 (32x32 for
+//                 16-byte types) shared-memory tiles, coalesced on both
 //                 sides, other modes enumerated by the grid;
 //  * gather     — strided views without a unit-stride mode: element-wise.
 // HBM-bound: algorithmic bytes = numel * (sizeof(src) + sizeof(dst)).
@@ -167,7 +167,7 @@ static int run_permute(const PermGeom &pg, const TS *x, TD *y, cudaStream_t s) {
         ModeGroup outer = drop_mode(g, 0, pg.b);
         int64_t ea = g.ext[0], eb = g.ext[pg.b];
         int64_t sxa = g.str[0][0], syb = g.str[1][pg.b];
-        constexpr int T = sizeof(TD) <= 4 ? 64 : 32;
+        constexpr int T = sizeof(TD) <= 8 ? 64 : 32;  // 32 KB (8-byte) or 16 KB (16-byte) tiles
         int64_t tiles_a = (ea + T - 1) / T, tiles_b = (eb + T - 1) / T;
         int64_t blocks = tiles_a * tiles_b * outer.size();
         if (blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "permute: too many tiles");
