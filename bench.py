@@ -58,10 +58,11 @@ def parse():
     ap.add_argument("--native-steps", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "peps", "serve", "config2", "kernel", "permute"],
+                    choices=["precision", "peps", "serve", "config2", "kernel", "permute", "hadamard"],
                     help="precision: the headline line; peps / serve: batching and serving forms; config2: "
                          "plain shapes that permute; kernel / permute: one contraction of the precision "
-                         "workload at --n / the permutation of A(a,b,c,d,e) with e = --perm-e (profiling cases)")
+                         "workload at --n / the permutation of A(a,b,c,d,e) with e = --perm-e (profiling cases); "
+                         "hadamard: broadcast product of a 4.3 GB array")
     ap.add_argument("--form", default="ozaki", help="form of --workload kernel")
     ap.add_argument("--perm-e", type=int, default=32, help="extent of label e in --workload permute")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="per offered rate in the serving sweep")
@@ -194,7 +195,7 @@ def max_over_ranks(x, ws):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -523,6 +524,51 @@ def permute_case(dev, e, steps, warmup):
             "bit_exact": bool(torch.equal(Y.data, x.permute(1, 3, 0, 2, 4)))}
 
 
+def hadamard_case(dev, steps, warmup):
+    """hadamard(a, b) of a(x, y) = 2^16 x 2^12 with a vector b(y), the scaling
+    step that follows a contraction in a simple update, in ComplexF64 and
+    ComplexF32. Algorithmic bytes = read a + write c (+ b). ComplexF64 does 6
+    FP64 flops per element (4 instructions with FMA) on GB300's ~1.25 TFLOP/s
+    FP64 pipe, so it is bound by that pipe rather than HBM; ComplexF32 is
+    HBM-bound."""
+    import torch
+
+    import muscle_gb300 as m
+
+    out = {}
+    _, hbm, kind = peaks()
+    for tdt, name in ((torch.complex128, "c64"), (torch.complex64, "c32")):
+        g = torch.Generator(device=dev)
+        g.manual_seed(0)
+        n0, n1 = 1 << 16, 1 << 12
+        a = torch.randn(n1, n0, dtype=tdt, device=dev, generator=g).t()
+        b = torch.randn(n1, dtype=tdt, device=dev, generator=g)
+        A, B = m.Tensor(a, ["x", "y"]), m.Tensor(b, ["y"])
+        C = m.Tensor(m.empty_colmajor([n0, n1], tdt, dev), ["x", "y"])
+        for _ in range(warmup):
+            m.hadamard_(C, A, B)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            m.hadamard_(C, A, B)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        es = a.element_size()
+        nb = 2 * a.numel() * es + b.numel() * es
+        want = a * b[None, :]
+        tol = 1e-15 if tdt == torch.complex128 else 1e-6
+        ok = bool((C.data - want).abs().max().item() <= tol * want.abs().max().item())
+        out[name] = {"bytes": nb, "ms": ms, "gbs": nb / (ms / 1e3) / 1e9, "frac_of_hbm": nb / (ms / 1e3) / 1e9 / hbm,
+                     "peak_kind": kind, "matches_torch": ok}
+        if tdt == torch.complex128:
+            out[name]["fp64_tflops"] = 6.0 * a.numel() / (ms / 1e3) / 1e12
+        del a, b, A, B, C, want
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -568,6 +614,9 @@ def main():
         elif args.workload == "permute":
             res = permute_case(dev, args.perm_e, args.steps, args.warmup)
             metric = "permutation kernel GB/s (profiling case)"
+        elif args.workload == "hadamard":
+            res = hadamard_case(dev, args.steps, args.warmup)
+            metric = "hadamard (broadcast product) GB/s"
         else:
             res = serve_bench(dev, [1000, 3000, 10000, 30000, 100000], args.serve_seconds)
             metric = "served contractions/s with p50/p99 ms (Poisson arrivals)"

@@ -108,6 +108,18 @@ int mgb_unary(mgb_plan plan, const void *X, void *Y, void *workspace,
 int mgb_permute(const mgb_tensor_desc *x, const mgb_tensor_desc *y,
                 const void *X, void *Y, void *stream);
 
+/* ---- Hadamard (broadcast element-wise) product: C = A .* B -----------------
+ * Replaces hadamard / hadamard! of BackendBase (src/Operations/hadamard.jl:
+ * 34-77) on device arrays. modes_b must be distinct and a subset of modes_a
+ * (hadamard.jl:10,24), B is broadcast along A's other labels, and C carries
+ * A's labels in A's order (hadamard.jl:23). The product is formed in the
+ * promoted type of A and B and stored in C's type; a complex product into a
+ * real C is rejected. C may alias A (hadamard!(a, a, b)) when the two have
+ * the same layout and element type; other overlaps are not allowed.     */
+int mgb_hadamard(const mgb_tensor_desc *a, const mgb_tensor_desc *b,
+                 const mgb_tensor_desc *c, const void *A, const void *B,
+                 void *C, void *stream);
+
 int mgb_plan_info_get(mgb_plan plan, mgb_plan_info *info);
 /* Phase timing for benchmarks. When enabled, mgb_contract records CUDA events
  * on its launch stream before its pre-pass kernels (scales, slices or

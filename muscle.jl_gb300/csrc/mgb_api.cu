@@ -72,16 +72,10 @@ int read_desc(const mgb_tensor_desc *d, Desc &out, const char *name) {
 
 // ---------------------------------------------------------------------------
 // Mode folding.
-struct ModeRec {
-    int label;
-    int64_t ext;
-    int64_t str[3];
-};
-
 // Builds a folded ModeGroup. `present[t]` marks tensors that carry the group.
 // Modes are ordered by |stride| in tensor `primary`, extent-1 modes dropped,
 // and neighbours merged when they are linear in every present tensor.
-static ModeGroup fold_group(std::vector<ModeRec> modes, const bool present[3], int primary) {
+ModeGroup fold_group(std::vector<ModeRec> modes, const bool present[3], int primary) {
     ModeGroup g;
     bool empty = false;
     std::vector<ModeRec> kept;
@@ -131,14 +125,14 @@ static int64_t min_stride_label(const Desc &d) {
     return lab;
 }
 
-static bool has_repeats(const Desc &d) {
+bool has_repeats(const Desc &d) {
     for (int i = 0; i < d.rank; ++i)
         for (int j = i + 1; j < d.rank; ++j)
             if (d.modes[i] == d.modes[j]) return true;
     return false;
 }
 
-static int find_mode(const Desc &d, int label) {
+int find_mode(const Desc &d, int label) {
     for (int i = 0; i < d.rank; ++i)
         if (d.modes[i] == label) return i;
     return -1;

@@ -76,6 +76,17 @@ struct Desc {
     int64_t str[kMaxRank];
 };
 int read_desc(const mgb_tensor_desc *d, Desc &out, const char *name);
+bool has_repeats(const Desc &d);
+int find_mode(const Desc &d, int label);  // position of `label` in d, or -1
+
+// One label of a contraction or broadcast with its extent and its stride in
+// up to three tensors (0 where the tensor lacks it).
+struct ModeRec {
+    int label;
+    int64_t ext;
+    int64_t str[3];
+};
+ModeGroup fold_group(std::vector<ModeRec> modes, const bool present[3], int primary);
 
 enum class PlanKind { Contraction, Unary };
 
@@ -138,6 +149,8 @@ int launch_plain_gemm(const ContractionPlan &p, const void *A, const void *B, vo
 int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C,
                  void *ws, cudaStream_t s, cudaEvent_t mid = nullptr);
 int launch_unary(const UnaryPlan &p, const void *X, void *Y, cudaStream_t s);
+int launch_hadamard(const ModeGroup &g, int ta, int tb, int tc, const void *A, const void *B, void *C,
+                    cudaStream_t s);
 int32_t *device_status_ptr();  // per-device status word
 uint64_t ozaki_workspace(ContractionPlan &p);
 void ozaki_setup(ContractionPlan &p);

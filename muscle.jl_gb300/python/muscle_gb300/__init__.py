@@ -32,6 +32,8 @@ from .ops import (
     contract_into,
     contraction_plan,
     device_status,
+    hadamard,
+    hadamard_,
     permutedims,
     promote_eltype,
     unary_einsum,

@@ -84,6 +84,7 @@ SIGNATURES = {
     "mgb_unary_plan": (_i32, [_P(_vp), _P(TensorDesc), _P(TensorDesc)]),
     "mgb_unary": (_i32, [_vp, _vp, _vp, _vp, _u64, _vp]),
     "mgb_permute": (_i32, [_P(TensorDesc), _P(TensorDesc), _vp, _vp, _vp]),
+    "mgb_hadamard": (_i32, [_P(TensorDesc), _P(TensorDesc), _P(TensorDesc), _vp, _vp, _vp, _vp]),
     "mgb_plan_info_get": (_i32, [_vp, _P(PlanInfo)]),
     "mgb_plan_workspace_size": (_i32, [_vp, _P(_u64)]),
     "mgb_plan_destroy": (_i32, [_vp]),

@@ -62,6 +62,12 @@ class Backend:
     def unary_einsum_(self, y, x):
         raise ArgumentError(f"`unary_einsum!` not implemented or not loaded for backend {type(self).__name__}")
 
+    def hadamard(self, a, b):
+        raise ArgumentError(f"`hadamard` not implemented or not loaded for backend {type(self).__name__}")
+
+    def hadamard_(self, c, a, b):
+        raise ArgumentError(f"`hadamard!` not implemented or not loaded for backend {type(self).__name__}")
+
     def __eq__(self, o):
         return type(self) is type(o) and self.__dict__ == o.__dict__
 

@@ -223,8 +223,38 @@ class BackendGB300(Backend):
         return y
 
 
+    # hadamard(::BackendBase, a, b) (src/Operations/hadamard.jl:34-40): the
+    # result has a's labels and a's element type
+    def hadamard(self, a: Tensor, b: Tensor) -> Tensor:
+        if a.ndim < b.ndim:
+            a, b = b, a
+        c = empty_colmajor(list(a.data.shape), a.dtype, a.data.device)
+        C = Tensor(c, list(a.inds))
+        self.hadamard_(C, a, b)
+        return C
+
+    # hadamard!(::BackendBase, c, a, b) (src/Operations/hadamard.jl:42-77)
+    def hadamard_(self, c: Tensor, a: Tensor, b: Tensor) -> Tensor:
+        if a.ndim < b.ndim:
+            a, b = b, a
+        _require_cuda(a.data, b.data, c.data)
+        if list(c.inds) != list(a.inds):
+            raise ArgumentError("hadamard!: inds(c) must equal inds(a)")
+        if any(i not in a.inds for i in b.inds):
+            raise ArgumentError("hadamard: inds(b) must be a subset of inds(a)")
+        modes = _modes_for(a.inds)
+        lib = _lib.load()
+        (ad, ka), (bd, kb), (cd, kc) = (_lib.make_desc(*_desc_args(a.data, a.inds, modes)),
+                                        _lib.make_desc(*_desc_args(b.data, b.inds, modes)),
+                                        _lib.make_desc(*_desc_args(c.data, c.inds, modes)))
+        check(lib.mgb_hadamard(ctypes.byref(ad), ctypes.byref(bd), ctypes.byref(cd), a.data.data_ptr(),
+                               b.data.data_ptr(), c.data.data_ptr(), _stream_handle(c.data.device)), lib)
+        return c
+
+
 for _f, _doms in (("binary_einsum", (DomainCUDA, DomainCUDA)), ("binary_einsum_", (DomainCUDA, DomainCUDA, DomainCUDA)),
-                  ("unary_einsum", (DomainCUDA,)), ("unary_einsum_", (DomainCUDA, DomainCUDA))):
+                  ("unary_einsum", (DomainCUDA,)), ("unary_einsum_", (DomainCUDA, DomainCUDA)),
+                  ("hadamard", (DomainCUDA, DomainCUDA)), ("hadamard_", (DomainCUDA, DomainCUDA, DomainCUDA))):
     register_rule(_f, _doms, BackendGB300)
 
 
@@ -286,6 +316,32 @@ def unary_einsum_(y: Tensor, x: Tensor) -> Tensor:
     backend = choose_backend(unary_einsum_, y.data, x.data)
     backend.unary_einsum_(y, x)
     return y
+
+
+def hadamard(a: Tensor, b: Tensor) -> Tensor:
+    """Broadcast element-wise product (src/Operations/hadamard.jl:7-13): the
+    operand of lower rank is broadcast along the other's labels; its labels
+    must be a subset of the other's."""
+    if a.ndim < b.ndim:
+        a, b = b, a
+    if any(i not in a.inds for i in b.inds):
+        raise ArgumentError("hadamard: inds(b) must be a subset of inds(a)")
+    backend = choose_backend(hadamard, a.data, b.data)
+    return backend.hadamard(a, b)
+
+
+def hadamard_(c: Tensor, a: Tensor, b: Tensor) -> Tensor:
+    """In-place broadcast product into ``c`` (src/Operations/hadamard.jl:19-28):
+    inds(c) == inds(a), inds(b) a subset of inds(a)."""
+    if a.ndim < b.ndim:
+        a, b = b, a
+    if list(c.inds) != list(a.inds):
+        raise ArgumentError("hadamard!: inds(c) must equal inds(a)")
+    if any(i not in a.inds for i in b.inds):
+        raise ArgumentError("hadamard!: inds(b) must be a subset of inds(a)")
+    backend = choose_backend(hadamard_, c.data, a.data, b.data)
+    backend.hadamard_(c, a, b)
+    return c
 
 
 def permutedims(t: Tensor, perm) -> Tensor:

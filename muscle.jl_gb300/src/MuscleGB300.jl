@@ -143,12 +143,36 @@ function Muscle.unary_einsum!(::BackendGB300, y::Tensor, x::Tensor)
     return y
 end
 
+# hadamard(::Backend, a, b)  (src/Operations/hadamard.jl:34-40): c has a's
+# labels and a's element type
+function Muscle.hadamard(be::BackendGB300, a::Tensor, b::Tensor)
+    ndims(a) >= ndims(b) || return Muscle.hadamard(be, b, a)
+    c = Tensor(similar(parent(a)), collect(inds(a)))
+    return Muscle.hadamard!(be, c, a, b)
+end
+
+# hadamard!(::Backend, c, a, b)  (src/Operations/hadamard.jl:42-77)
+function Muscle.hadamard!(be::BackendGB300, c::Tensor, a::Tensor, b::Tensor)
+    ndims(a) >= ndims(b) || return Muscle.hadamard!(be, c, b, a)
+    m = modemap(a, b, c)
+    aa, ab, ac = descarrays(a, m), descarrays(b, m), descarrays(c, m)
+    GC.@preserve aa ab ac begin
+        da, db, dc = Ref(desc(a, aa)), Ref(desc(b, ab)), Ref(desc(c, ac))
+        check(ccall((:mgb_hadamard, libmgb), Cint,
+                    (Ref{TensorDesc}, Ref{TensorDesc}, Ref{TensorDesc}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid},
+                     CUDA.CUstream),
+                    da, db, dc, parent(a), parent(b), parent(c), CUDA.stream()))
+    end
+    return c
+end
+
 """
     MuscleGB300.enable!()
 
 Make `BackendGB300` the rule for device-resident operands, replacing the
 `BackendCuTENSOR` / `BackendOMEinsum` rules of
-src/Operations/binary_einsum.jl:21,30 and src/Operations/unary_einsum.jl:21,24.
+src/Operations/binary_einsum.jl:21,30 and src/Operations/unary_einsum.jl:21,24,
+and the `BackendBase` rules of src/Operations/hadamard.jl:4-5.
 Muscle defines those methods itself, so they are replaced at run time (method
 overwriting is not allowed while a package precompiles). Without this call
 `with_backend(f, BackendGB300())` still selects the backend.
@@ -159,6 +183,8 @@ function enable!()
         choose_backend_rule(::typeof(binary_einsum!), ::DomainCUDA, ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
         choose_backend_rule(::typeof(unary_einsum), ::DomainCUDA) = $(BackendGB300)()
         choose_backend_rule(::typeof(unary_einsum!), ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
+        choose_backend_rule(::typeof(hadamard), ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
+        choose_backend_rule(::typeof(hadamard!), ::DomainCUDA, ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
     end
     return nothing
 end

@@ -182,6 +182,34 @@ def unary(x, ix, iy):
     return np.einsum(spec, x)
 
 
+def hadamard(a, ia, b, ib):
+    """BackendBase hadamard (src/Operations/hadamard.jl:34-77): c = a .* b with
+    the operand of lower rank broadcast along the other's labels; c has a's
+    labels and a's element type (c = copy(a), then c .= a .* b), so a complex
+    product into a real a is an error (Julia's InexactError).
+
+    b is brought into a's label order by labels. The reference does this with
+    permutedims(b, findperm(inds(b), inds(a) ∩ inds(b))) (hadamard.jl:66-69),
+    which equals the label-wise order whenever that permutation is its own
+    inverse (every case of its tests: rank(b) <= 2); for a 3-cycle of labels it
+    would use the inverse permutation."""
+    ia, ib = list(ia), list(ib)
+    if a.ndim < b.ndim:
+        a, ia, b, ib = b, ib, a, ia
+    if any(i not in ia for i in ib):
+        raise ArgumentError("hadamard: inds(b) must be a subset of inds(a)")
+    if b.ndim == 0:
+        prod = a * b
+    else:
+        order = [i for i in ia if i in ib]
+        bb = np.transpose(b, [ib.index(i) for i in order])
+        shape = [a.shape[d] if ia[d] in ib else 1 for d in range(len(ia))]
+        prod = a * bb.reshape(shape, order="F")
+    if np.iscomplexobj(prod) and not np.iscomplexobj(a) and np.any(np.imag(prod) != 0):
+        raise ArgumentError("hadamard: InexactError (complex product into a real array)")
+    return np.array(np.real(prod) if not np.iscomplexobj(a) else prod, dtype=a.dtype, order="F"), ia
+
+
 def exact_entries(a, ia, b, ib, ic, positions):
     """Exact (rational) values of selected output entries, used to bound the
     oracle's own rounding error. positions: list of index tuples of C."""

@@ -1,5 +1,5 @@
 """Writes kat_cases.json: the known-answer assertions of Muscle.jl's own tests
-for binary_einsum / unary_einsum / permutedims, restated as data.
+for binary_einsum / unary_einsum / permutedims / hadamard, restated as data.
 
 Every case records where its assertion lives in the Muscle.jl test suite.
 Inputs in those tests are `ones`/`fill` arrays, so expected results are exact
@@ -123,6 +123,28 @@ uadd("partial trace iji->j inplace", f"{O}:98-100", X, res(["j"], [3], 2.0), inp
 cases.append({"kind": "permute", "name": "permutedims 1:24", "ref": "test/unit/tensor.jl:447-465",
               "x": {"shape": [2, 3, 4], "inds": ["i", "j", "k"], "iota": True, "dtype": "float64"},
               "perm": ["k", "i", "j"], "expect": {"inds": ["k", "i", "j"], "shape": [4, 2, 3]}})
+
+# hadamard / hadamard! on ones(2, 3, 4) (test/unit/operations/hadamard.jl). "b_broadcast":
+# the test asserts that every slice of c along b's labels equals b's entry there.
+H = "test/unit/operations/hadamard.jl"
+A = arr([2, 3, 4], ["i", "j", "k"])
+
+
+def hadd(name, lines, b, expect):
+    for inplace in (False, True):
+        cases.append({"kind": "hadamard", "name": name + (" inplace" if inplace else ""), "ref": f"{H}:{lines}",
+                      "a": A, "b": b, "inplace": inplace, "expect": expect})
+
+
+hadd("tensor - scalar", "4-19", arr([], [], 2.0), res(["i", "j", "k"], [2, 3, 4], 2.0))
+for lab, vals, lines in (("i", [1.0, 2.0], "24-40"), ("j", [1.0, 2.0, 3.0], "42-58"), ("k", [1.0, 2.0, 3.0, 4.0], "60-76")):
+    hadd(f"tensor - vector {lab}", lines, {"shape": [len(vals)], "inds": [lab], "values": vals, "dtype": "float64"},
+         {"inds": ["i", "j", "k"], "shape": [2, 3, 4], "formula": "b_broadcast"})
+# Float64[1 2 3; 4 5 6] in column-major order
+hadd("tensor - matrix bcast", "79-101", {"shape": [2, 3], "inds": ["i", "j"], "values": [1.0, 4.0, 2.0, 5.0, 3.0, 6.0],
+                                         "dtype": "float64"},
+     {"inds": ["i", "j", "k"], "shape": [2, 3, 4], "formula": "b_broadcast"})
+hadd("tensor - tensor", "103-117", arr([2, 3, 4], ["i", "j", "k"], 2.0), res(["i", "j", "k"], [2, 3, 4], 2.0))
 
 path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "kat_cases.json")
 with open(path, "w") as f:

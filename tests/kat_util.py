@@ -10,6 +10,8 @@ def fill_value(f):
 
 def make_array(spec):
     dt = NP[spec["dtype"]]
+    if "values" in spec:
+        return np.array(np.array(spec["values"], dtype=dt).reshape(spec["shape"], order="F"), order="F")
     if spec.get("iota"):
         n = int(np.prod(spec["shape"]))
         return np.array(np.arange(1, n + 1, dtype=dt).reshape(spec["shape"], order="F"), order="F")
@@ -30,4 +32,16 @@ def expected_binary(case, exp, a, b):
             for k in range(4):
                 for l in range(5):
                     c[i, k, l] += a[i, j, k] * b[k, l, j]
+    return c
+
+
+def expected_hadamard(exp, b, ib):
+    """Expected c of a hadamard case on a = ones: a fill, or b broadcast along
+    c's labels (each slice of c at b's coordinates equals b's entry there)."""
+    if "fill" in exp:
+        return np.full(exp["shape"], fill_value(exp["fill"]))
+    c = np.zeros(exp["shape"], dtype=b.dtype)
+    for idx in np.ndindex(*exp["shape"]):
+        pos = dict(zip(exp["inds"], idx))
+        c[idx] = b[tuple(pos[i] for i in ib)]
     return c

@@ -53,6 +53,32 @@ def test_kat_unary(kat_cases):
         assert np.array_equal(y, np.full(case["expect"]["shape"], case["expect"]["fill"])), case["name"]
 
 
+def test_kat_hadamard(kat_cases):
+    from tests.kat_util import expected_hadamard
+
+    hs = [c for c in kat_cases if c["kind"] == "hadamard"]
+    assert len(hs) == 12
+    for case in hs:
+        a, b = make_array(case["a"]), make_array(case["b"])
+        c, ic = ref.hadamard(a, case["a"]["inds"], b, case["b"]["inds"])
+        exp = case["expect"]
+        assert ic == exp["inds"] and list(c.shape) == exp["shape"], case["name"]
+        assert np.array_equal(c, expected_hadamard(exp, b, case["b"]["inds"])), case["name"]
+        # operand order does not matter: the operand of lower rank is broadcast
+        c2, ic2 = ref.hadamard(b, case["b"]["inds"], a, case["a"]["inds"])
+        assert ic2 == ic and np.array_equal(c2, c)
+
+
+def test_hadamard_errors_and_types():
+    a = np.ones((2, 3))
+    with pytest.raises(ref.ArgumentError):
+        ref.hadamard(a, ["i", "j"], np.ones(4), ["k"])
+    c, _ = ref.hadamard(a.astype(np.float32), ["i", "j"], np.full(3, 0.5), ["j"])
+    assert c.dtype == np.float32 and np.all(c == 0.5)
+    with pytest.raises(ref.ArgumentError):
+        ref.hadamard(a, ["i", "j"], np.full(3, 1j), ["j"])
+
+
 def test_kat_permute(kat_cases):
     case = [c for c in kat_cases if c["kind"] == "permute"][0]
     x = make_array(case["x"])
