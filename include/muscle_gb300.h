@@ -153,7 +153,7 @@ int mgb_group_workspace_size(mgb_group group, uint64_t *bytes);
 int mgb_group_execute(mgb_group group, void *workspace,
                       uint64_t workspace_bytes, void *stream);
 /* Tile schedule of the batched tensor-core launches: per member, an index
- * 0..5 into the rasterisation bands {1, 2, 4, 8, 16, 32} (row tiles walked
+ * 0..5 into the rasterisation bands {1, 2, 3, 4, 8, 16} (row tiles walked
  * together across all column tiles); a bucket takes its first member's
  * value; -1 = default band (16). Written by the host-side autotuner.      */
 int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan);

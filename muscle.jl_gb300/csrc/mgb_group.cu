@@ -32,7 +32,7 @@ struct Single {
     uint64_t ws_off;
 };
 
-const int kBands[6] = {1, 2, 4, 8, 16, 32};
+const int kBands[6] = {1, 2, 3, 4, 8, 16};
 
 }  // namespace
 

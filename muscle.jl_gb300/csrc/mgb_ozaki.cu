@@ -61,8 +61,15 @@ constexpr int OZ_KC = 256;     // BF16X3: embedded k between readouts
 constexpr int OZ_BM = 128;     // rows of A per CTA (TMEM lanes)
 constexpr int OZ_BK = 32;      // k per stage (64-byte swizzled rows)
 constexpr int OZ_EPI_WARPS = 8;
-constexpr int OZ_GROUP_M = 8;  // row tiles per rasterisation band
-constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;
+// Row tiles per rasterisation band. The resident CTAs drift apart in k over
+// many waves, so L2 keeps a band's A slices only while they are small: on the
+// 8192^3 ComplexF64 case (S = 6) DRAM traffic per launch is 222 GB for bands
+// of 1, 135 GB for 2, 124 GB for 3, 145 GB for 4 and 187-224 GB for 8.
+constexpr int OZ_GROUP_M = 3;
+// warp 0 TMA, warp 1 MMA issuer (and TMEM owner), warps 2..9 epilogue,
+// warp 10 second MMA issuer
+constexpr int OZ_THREADS = 96 + 32 * OZ_EPI_WARPS;
+constexpr int OZ_ISSUER2_WARP = 2 + OZ_EPI_WARPS;
 constexpr int OZ_A_TILE = OZ_BM * OZ_BK * 2;  // 8192 bytes per slice
 constexpr int OZ_SMEM_BUDGET = 220 * 1024;
 constexpr int OZ_MAX_STAGES = 6;
@@ -181,6 +188,15 @@ __device__ __forceinline__ void tc_ld16_issue(uint32_t taddr, uint32_t *v) {
         : "r"(taddr)
         : "memory");
 }
+// zeroes 16 consecutive columns of this warp's 32 lanes (no wait)
+__device__ __forceinline__ void tc_st16_zero(uint32_t taddr) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr),
+        "r"(0u)
+        : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 // NC consecutive columns (a multiple of 16), then wait for the loads
 template <int NC>
 __device__ __forceinline__ void tc_ld(uint32_t taddr, uint32_t (&v)[NC]) {
@@ -506,16 +522,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     static_assert(BN * S <= BANK && TCOLS <= 512, "two banks must fit in TMEM");
     static_assert(BN * S <= 256, "one MMA covers at most 256 columns");
     static_assert(HALF % 16 == 0, "epilogue reads 16 columns at a time");
+    // MMA-issuing threads. Each mbarrier poll by an issuing thread stalls it
+    // for ~150 cycles while the tensor core's queue holds only ~200 cycles of
+    // MMAs, so a single issuer leaves a bubble at every k block. Two issuers
+    // (warps 1 and 10) take alternate k blocks and keep the queue fed while
+    // the other polls. Their MMAs into a bank interleave in an unspecified
+    // order, which changes nothing for the exact integer sums of the OZAKI
+    // form; BF16X3 sums round, so it keeps one issuer and stays deterministic.
+    constexpr int NI = EXACT ? 2 : 1;
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + NST * STAGE);
     uint64_t *full = bars;               // [NST]
     uint64_t *empty = bars + NST;        // [NST]
-    uint64_t *acc_full = bars + 2 * NST; // [2] bank filled (one commit)
-    uint64_t *acc_empty = acc_full + 2;  // [2] bank read (one arrive per epilogue warp)
-    uint64_t *done = acc_empty + 2;
-    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    uint64_t *acc_full = bars + 2 * NST; // [2] bank filled (one commit per issuer)
+    uint64_t *acc_empty = acc_full + 2;  // [2] bank read and cleared (one arrive per epilogue warp)
+    uint64_t *done = acc_empty + 2;      // [2] per issuer: all its MMAs complete
+    uint32_t *tmem_slot = (uint32_t *)(done + 2);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
@@ -543,10 +567,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             mbar_init(smem_u32(empty + s), 1);
         }
         for (int b = 0; b < 2; ++b) {
-            mbar_init(smem_u32(acc_full + b), 1);
+            mbar_init(smem_u32(acc_full + b), NI);
             mbar_init(smem_u32(acc_empty + b), OZ_EPI_WARPS);
+            mbar_init(smem_u32(done + b), 1);
         }
-        mbar_init(smem_u32(done), 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -564,6 +588,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const uint32_t tmem = *tmem_slot;
     const int nkb = args.nkb, kcb = args.kcb;
     const int nchunks = (nkb + kcb - 1) / kcb;
+    // Every MMA accumulates (the issuers' order within a bank is free); the
+    // epilogue warps clear both banks here and each bank again after reading it.
+    if (warp >= 2 && warp < 2 + OZ_EPI_WARPS) {
+        const int q = warp % 4, h = (warp - 2) / 4;
+        for (int c = 0; c < TCOLS / 2; c += 16) tc_st16_zero(tmem + ((uint32_t)(32 * q) << 16) + h * (TCOLS / 2) + c);
+        tc_wait_st();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
@@ -584,47 +618,48 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             for (int kb = max(0, issued - NST); kb < issued; ++kb)
                 mbar_drain(smem_u32(full + kb % NST), (kb / NST) & 1);
         }
-    } else if (warp == 1) {
-        // ---------------- MMA issuer ----------------
+    } else if (warp == 1 || (NI == 2 && warp == OZ_ISSUER2_WARP)) {
+        // ---------------- MMA issuers ----------------
+        // Issuer `me` takes the k blocks kb with kb % NI == me (kcb is even).
+        // Per chunk c it waits until the epilogue has read and cleared the
+        // bank's previous chunk (c - 2), issues its k blocks, and commits the
+        // chunk's acc_full barrier once (also when it owns no k block of it).
         if (lane == 0) {
+            const int me = warp == 1 ? 0 : 1;
             bool ok = true;
-            for (int kb = 0; kb < nkb && ok; ++kb) {
-                const int s = kb % NST;
-                const int c = kb / kcb;          // chunk
-                const int kin = kb - c * kcb;    // k block inside the chunk
+            for (int c = 0; c < nchunks && ok; ++c) {
                 const uint32_t bank = (uint32_t)c & 1u;
-                if (!mbar_wait(smem_u32(full + s), (kb / NST) & 1, abort_flag, args.status)) {
+                if (!mbar_wait(smem_u32(acc_empty + bank), ((uint32_t)(c >> 1) & 1u) ^ 1u, abort_flag, args.status)) {
                     ok = false;
                     break;
                 }
-                // a chunk starts in a bank once the epilogue has read the chunk
-                // two before it (the wait passes at once for the first two)
-                if (kin == 0 &&
-                    !mbar_wait(smem_u32(acc_empty + bank), ((uint32_t)(c >> 1) & 1u) ^ 1u, abort_flag, args.status)) {
-                    ok = false;
-                    break;
+                const int kb1 = min(nkb, (c + 1) * kcb);
+                for (int kb = c * kcb + me; kb < kb1; kb += NI) {
+                    const int s = kb % NST;
+                    if (!mbar_wait(smem_u32(full + s), (kb / NST) & 1, abort_flag, args.status)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_base = smem_u32(smem + s * STAGE);
+                    const uint64_t ad0 = sw64_desc(a_base);
+                    const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
+                    const uint32_t d0 = tmem + bank * BANK;
+#pragma unroll
+                    for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
+#pragma unroll
+                        for (int i = 0; i < S; ++i)
+                            tc_mma(d0 + BN * i, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
+                                   bd0 + (uint64_t)((k16 * 32) >> 4), oz_idesc(BN * (S - i)), 1u);
+                    tc_commit(smem_u32(empty + s));
                 }
-                tc_fence_after();
-                const uint32_t a_base = smem_u32(smem + s * STAGE);
-                const uint64_t ad0 = sw64_desc(a_base);
-                const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
-                const uint32_t d0 = tmem + bank * BANK;
-                const uint32_t first = kin == 0 ? 0u : 1u;
-#pragma unroll
-                for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
-#pragma unroll
-                    for (int i = 0; i < S; ++i)
-                        tc_mma(d0 + BN * i, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
-                               bd0 + (uint64_t)((k16 * 32) >> 4), oz_idesc(BN * (S - i)),
-                               (k16 == 0 && i == 0) ? first : 1u);
-                tc_commit(smem_u32(empty + s));
-                if (kin == kcb - 1 || kb == nkb - 1) tc_commit(smem_u32(acc_full + bank));
+                if (ok) tc_commit(smem_u32(acc_full + bank));
             }
             // wait for every MMA this thread issued before TMEM is released
-            tc_commit(smem_u32(done));
-            mbar_drain(smem_u32(done), 0);
+            tc_commit(smem_u32(done + me));
+            mbar_drain(smem_u32(done + me), 0);
         }
-    } else {
+    } else if (warp < 2 + OZ_EPI_WARPS) {
         // ---------------- epilogue ----------------
         const int q = warp % 4;        // TMEM lane quarter this warp may access
         const int h = (warp - 2) / 4;  // column half (HALF columns) of each group
@@ -661,7 +696,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 for (int g = 0; g < S; ++g) {
                     uint32_t v[HALF];
                     tc_ld<HALF>(tb + BN * g, v);
-                    if (g == S - 1) {  // every group of the bank is in registers
+#pragma unroll
+                    for (int c = 0; c < HALF; c += 16) tc_st16_zero(tb + BN * g + c);
+                    if (g == S - 1) {  // every group of the bank read and cleared
+                        tc_wait_st();
                         tc_fence_before();
                         __syncwarp();
                         if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));
@@ -688,6 +726,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 tc_ld<HALF>(tb, v0);
                 tc_ld<HALF>(tb + BN, v1);
                 tc_ld<HALF>(tb + 2 * BN, v2);
+#pragma unroll
+                for (int g = 0; g < 3; ++g)
+#pragma unroll
+                    for (int c = 0; c < HALF; c += 16) tc_st16_zero(tb + BN * g + c);
+                tc_wait_st();
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));

@@ -19,7 +19,7 @@ import torch
 from .grouped import Group
 
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "muscle_gb300", "autotune.json")
-BANDS = (1, 3, 5)  # 2, 8, 32 row tiles per band
+BANDS = (1, 2, 4)  # 2, 3, 8 row tiles per band
 
 
 def _class_key(c, a, b) -> str:

@@ -66,7 +66,7 @@ class Group:
         return sum(p.flops for p in self.plans)
 
     def set_bands(self, bands):
-        """Rasterisation band index (0..5 -> 1,2,4,8,16,32 row tiles) per item."""
+        """Rasterisation band index (0..5 -> 1,2,3,4,8,16 row tiles) per item."""
         n = len(self.items)
         arr = (ctypes.c_int32 * n)(*bands)
         lib = _lib.load()
