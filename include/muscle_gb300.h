@@ -152,6 +152,14 @@ int mgb_group_update(mgb_group group, const void *const *A,
 int mgb_group_workspace_size(mgb_group group, uint64_t *bytes);
 int mgb_group_execute(mgb_group group, void *workspace,
                       uint64_t workspace_bytes, void *stream);
+/* The members of part `part` of `nparts` (0 <= part < nparts). The work units
+ * (batched buckets and single members) are dealt, largest first, to the part
+ * with the least work so far. Parts touch disjoint outputs and workspace
+ * slices, so they may run at the same time on different streams, e.g. as
+ * parallel branches of one CUDA graph. No counterpart in the reference.   */
+int mgb_group_execute_part(mgb_group group, int32_t part, int32_t nparts,
+                           void *workspace, uint64_t workspace_bytes,
+                           void *stream);
 /* Tile schedule of the batched tensor-core launches: per member, an index
  * 0..5 into the rasterisation bands {1, 2, 3, 4, 8, 16} (row tiles walked
  * together across all column tiles); a bucket takes its first member's

@@ -171,24 +171,61 @@ int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan) {
     return MGB_OK;
 }
 
+// Work units (buckets, then singles) of part `part` of `nparts`: units are
+// dealt in decreasing order of flops to the part with the least work so far.
+static std::vector<int> part_units(const mgb_group_s *g, int part, int nparts) {
+    const int nb = (int)g->buckets.size(), nu = nb + (int)g->singles.size();
+    std::vector<std::pair<double, int>> w(nu);
+    for (int u = 0; u < nu; ++u) {
+        const ContractionPlan &cp = u < nb ? g->buckets[u].cp : g->plans[g->singles[u - nb].member]->cp;
+        w[u] = {(double)cp.M * (double)cp.N * (double)std::max<int64_t>(cp.K, 1) * (double)cp.L, u};
+    }
+    std::stable_sort(w.begin(), w.end(), [](const std::pair<double, int> &x, const std::pair<double, int> &y) {
+        return x.first > y.first;
+    });
+    std::vector<double> load(nparts, 0.0);
+    std::vector<int> mine;
+    for (auto &x : w) {
+        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[k] += x.first;
+        if (k == part) mine.push_back(x.second);
+    }
+    std::sort(mine.begin(), mine.end());
+    return mine;
+}
+
+static int run_unit(mgb_group g, int u, void *workspace, cudaStream_t s) {
+    const int nb = (int)g->buckets.size();
+    if (u < nb) {
+        Bucket &b = g->buckets[u];
+        return b.cp.form == MGB_FORM_PLAIN ? launch_plain_gemm(b.cp, nullptr, nullptr, nullptr, s)
+                                           : launch_ozaki(b.cp, nullptr, nullptr, nullptr, (char *)workspace + b.ws_off, s);
+    }
+    const Single &m = g->singles[u - nb];
+    const mgb_plan p = g->plans[m.member];
+    void *w = p->cp.ws_bytes ? (char *)workspace + m.ws_off : nullptr;
+    return mgb_contract(p, g->A[m.member], g->B[m.member], g->C[m.member], w, p->cp.ws_bytes, s);
+}
+
 int mgb_group_execute(mgb_group group, void *workspace, uint64_t workspace_bytes, void *stream) {
+    return mgb_group_execute_part(group, 0, 1, workspace, workspace_bytes, stream);
+}
+
+int mgb_group_execute_part(mgb_group group, int32_t part, int32_t nparts, void *workspace, uint64_t workspace_bytes,
+                           void *stream) {
     if (!group) return fail(MGB_ERR_ARGUMENT, "group: null argument");
+    if (nparts < 1 || part < 0 || part >= nparts) return fail(MGB_ERR_ARGUMENT, "group: part out of range");
     if (workspace_bytes < group->ws_bytes || (group->ws_bytes && !workspace))
         return fail(MGB_ERR_WORKSPACE, "group workspace smaller than mgb_group_workspace_size");
     cudaStream_t s = (cudaStream_t)stream;
-    for (auto &b : group->buckets) {
-        int st = b.cp.form == MGB_FORM_PLAIN
-                     ? launch_plain_gemm(b.cp, nullptr, nullptr, nullptr, s)
-                     : launch_ozaki(b.cp, nullptr, nullptr, nullptr, (char *)workspace + b.ws_off, s);
-        if (st) return st;
+    if (nparts == 1) {
+        const int nu = (int)(group->buckets.size() + group->singles.size());
+        for (int u = 0; u < nu; ++u)
+            if (int st = run_unit(group, u, workspace, s)) return st;
+        return MGB_OK;
     }
-    for (auto &m : group->singles) {
-        const mgb_plan p = group->plans[m.member];
-        void *w = p->cp.ws_bytes ? (char *)workspace + m.ws_off : nullptr;
-        int st = mgb_contract(p, group->A[m.member], group->B[m.member], group->C[m.member], w, p->cp.ws_bytes,
-                              stream);
-        if (st) return st;
-    }
+    for (int u : part_units(group, part, nparts))
+        if (int st = run_unit(group, u, workspace, s)) return st;
     return MGB_OK;
 }
 

@@ -534,14 +534,27 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + NST * STAGE);
-    uint64_t *full = bars;               // [NST]
-    uint64_t *empty = bars + NST;        // [NST]
-    uint64_t *acc_full = bars + 2 * NST; // [2] bank filled (one commit per issuer)
+    uint64_t *full = bars;               // [2 NST] see full_idx
+    uint64_t *empty = bars + 2 * NST;    // [NST]
+    uint64_t *acc_full = bars + 3 * NST; // [2] bank filled (one commit per issuer)
     uint64_t *acc_empty = acc_full + 2;  // [2] bank read and cleared (one arrive per epilogue warp)
     uint64_t *done = acc_empty + 2;      // [2] per issuer: all its MMAs complete
     uint32_t *tmem_slot = (uint32_t *)(done + 2);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
+    // Stage-landed barriers. Each one is waited on by a single issuer and in
+    // order of its phases: an mbarrier parity wait cannot tell phase r from
+    // phase r - 2, so a waiter that could run two phases ahead of a barrier
+    // would pass early. With two issuers and an odd stage count the rounds of
+    // a stage alternate between the issuers, so every stage gets one barrier
+    // per issuer (index 2 s + kb % 2) and each of those is used every other
+    // round; otherwise stage s always has the same issuer (index 2 s + s % 2,
+    // or 2 s for one issuer), used every round.
+    auto full_idx = [](int kb) { return 2 * (kb % NST) + (NI == 2 ? (kb & 1) : 0); };
+    auto full_par = [](int kb) {
+        const uint32_t r = (uint32_t)(kb / NST);
+        return (NI == 2 && (NST & 1)) ? (r >> 1) & 1u : r & 1u;
+    };
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     // Grouped rasterisation: consecutive CTAs walk a band of `band` row tiles
     // across all column tiles, so the slices of A and B they read are shared
@@ -563,7 +576,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 
     if (tid == 0) {
         for (int s = 0; s < NST; ++s) {
-            mbar_init(smem_u32(full + s), 1);
+            mbar_init(smem_u32(full + 2 * s), 1);
+            mbar_init(smem_u32(full + 2 * s + 1), 1);
             mbar_init(smem_u32(empty + s), 1);
         }
         for (int b = 0; b < 2; ++b) {
@@ -608,15 +622,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 uint32_t round = kb / NST;
                 if (!mbar_wait(smem_u32(empty + s), (round & 1) ^ 1, abort_flag, args.status)) break;
                 uint8_t *st = smem + s * STAGE;
-                mbar_expect_tx(smem_u32(full + s), STAGE);
-                tma_load_3d(smem_u32(st), &tmA, kb * OZ_BK, (int)m0, l * S, smem_u32(full + s));
-                tma_load_3d(smem_u32(st + S * OZ_A_TILE), &tmB, kb * OZ_BK, (int)n0, l * S,
-                            smem_u32(full + s));
+                const uint32_t fb = smem_u32(full + full_idx(kb));
+                mbar_expect_tx(fb, STAGE);
+                tma_load_3d(smem_u32(st), &tmA, kb * OZ_BK, (int)m0, l * S, fb);
+                tma_load_3d(smem_u32(st + S * OZ_A_TILE), &tmB, kb * OZ_BK, (int)n0, l * S, fb);
                 issued = kb + 1;
             }
             // make sure no bulk copy is still writing into shared memory
             for (int kb = max(0, issued - NST); kb < issued; ++kb)
-                mbar_drain(smem_u32(full + kb % NST), (kb / NST) & 1);
+                mbar_drain(smem_u32(full + full_idx(kb)), full_par(kb));
         }
     } else if (warp == 1 || (NI == 2 && warp == OZ_ISSUER2_WARP)) {
         // ---------------- MMA issuers ----------------
@@ -636,7 +650,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 const int kb1 = min(nkb, (c + 1) * kcb);
                 for (int kb = c * kcb + me; kb < kb1; kb += NI) {
                     const int s = kb % NST;
-                    if (!mbar_wait(smem_u32(full + s), (kb / NST) & 1, abort_flag, args.status)) {
+                    if (!mbar_wait(smem_u32(full + full_idx(kb)), full_par(kb), abort_flag, args.status)) {
                         ok = false;
                         break;
                     }

@@ -17,7 +17,7 @@ import torch
 
 from . import _lib
 from ._lib import ArgumentError, check
-from .ops import _require_cuda, _stream_handle, contraction_plan
+from .ops import _require_cuda, contraction_plan
 from .tensor import Tensor
 
 
@@ -83,22 +83,45 @@ class Group:
         lib = _lib.load()
         check(lib.mgb_group_update(self.handle, *self._pointer_arrays()), lib)
 
-    def execute(self, stream: torch.cuda.Stream | None = None):
+    def execute(self, stream: torch.cuda.Stream | None = None, parts: int = 1):
+        """Runs every member on `stream` (default: the current stream). With
+        parts > 1 the members are split into that many parts of about equal
+        work, run on side streams forked from and joined back into `stream`
+        (the parts write disjoint outputs and workspace slices)."""
         lib = _lib.load()
-        st = stream.cuda_stream if stream is not None else _stream_handle(self.device)
-        check(lib.mgb_group_execute(self.handle, self.workspace.data_ptr(), self.workspace_bytes, st), lib)
+        main = stream if stream is not None else torch.cuda.current_stream(self.device)
+        if parts <= 1:
+            check(lib.mgb_group_execute(self.handle, self.workspace.data_ptr(), self.workspace_bytes,
+                                        main.cuda_stream), lib)
+            return
+        side = self._side_streams(parts)
+        for ss in side:
+            ss.wait_stream(main)
+        for i, ss in enumerate(side):
+            check(lib.mgb_group_execute_part(self.handle, i, parts, self.workspace.data_ptr(), self.workspace_bytes,
+                                             ss.cuda_stream), lib)
+        for ss in side:
+            main.wait_stream(ss)
 
-    def capture(self) -> torch.cuda.CUDAGraph:
-        """Warm up once, then record execute() into a CUDA graph."""
+    def _side_streams(self, parts):
+        cache = getattr(self, "_side", None)
+        if cache is None or len(cache) != parts:
+            cache = [torch.cuda.Stream(self.device) for _ in range(parts)]
+            self._side = cache
+        return cache
+
+    def capture(self, parts: int = 1) -> torch.cuda.CUDAGraph:
+        """Warm up once, then record execute() into a CUDA graph (with parts > 1
+        the parts become parallel branches of the graph)."""
         s = torch.cuda.Stream(self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):
-            self.execute(s)
+            self.execute(s, parts)
         torch.cuda.current_stream(self.device).wait_stream(s)
         torch.cuda.synchronize(self.device)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            self.execute(torch.cuda.current_stream(self.device))
+            self.execute(torch.cuda.current_stream(self.device), parts)
         return g
 
     def __del__(self):
