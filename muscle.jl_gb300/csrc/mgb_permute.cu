@@ -94,7 +94,7 @@ __global__ void k_transpose(const TS *__restrict__ x, TD *__restrict__ y, ModeGr
     int tx = threadIdx.x % 32, ty = threadIdx.x / 32;  // 32 x 8
 #pragma unroll
     for (int bb = 0; bb < T; bb += 32) {
-#pragma unroll 4
+#pragma unroll
         for (int r = ty; r < T; r += 8) {
             int64_t ia = a0 + r, ib = b0 + bb + tx;
             if (ia < ea && ib < eb) tile[r][bb + tx] = Conv<TS, TD>::f(__ldg(xo + ia * sxa + ib));
@@ -103,7 +103,7 @@ __global__ void k_transpose(const TS *__restrict__ x, TD *__restrict__ y, ModeGr
     __syncthreads();
 #pragma unroll
     for (int aa = 0; aa < T; aa += 32) {
-#pragma unroll 4
+#pragma unroll
         for (int r = ty; r < T; r += 8) {
             int64_t ib = b0 + r, ia = a0 + aa + tx;
             if (ia < ea && ib < eb) yo[ia + ib * syb] = tile[aa + tx][r];
