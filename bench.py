@@ -384,11 +384,14 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
 
 
 def config2_bench(dev, steps=3):
-    """Plain native FP64/ComplexF64 contractions with index orders that force
-    permutation: (2a) A(a,b,c,d,e) 64x96x64x48x32, B(e,c,f,a) 32x64x128x64 -> (b,d,f);
-    (2b) MPS bond A(l,p,r) 512x4x512, B(r,q,s) 512x4x512 -> (l,p,q,s). Reports the
-    permutation kernel's HBM bandwidth on 2a's A (the permute BackendBase does)
-    and each form's time; the plain form reads the strided operands directly."""
+    """Plain native FP64/ComplexF64 contractions, and the emulated form beside
+    them: (1) A(i,j,k,l) x B(k,m,l,n) -> (i,j,m,n), every extent 32 (the
+    reference's own CPU-sized case; B needs a permutation on the host path);
+    with index orders that force permutation, (2a) A(a,b,c,d,e) 64x96x64x48x32,
+    B(e,c,f,a) 32x64x128x64 -> (b,d,f) and (2b) the MPS bond A(l,p,r) 512x4x512,
+    B(r,q,s) 512x4x512 -> (l,p,q,s). Reports the permutation kernel's HBM
+    bandwidth on 2a's A (the permute BackendBase does) and each form's time;
+    the plain form reads the strided operands directly."""
     import ctypes
 
     import torch
@@ -401,7 +404,9 @@ def config2_bench(dev, steps=3):
     gen = torch.Generator(device=dev)
     gen.manual_seed(0)
     res = {}
-    cases = {"2a": (["a", "b", "c", "d", "e"], [64, 96, 64, 48, 32], ["e", "c", "f", "a"], [32, 64, 128, 64],
+    cases = {"1": (["i", "j", "k", "l"], [32, 32, 32, 32], ["k", "m", "l", "n"], [32, 32, 32, 32],
+                   ["i", "j", "m", "n"]),
+             "2a": (["a", "b", "c", "d", "e"], [64, 96, 64, 48, 32], ["e", "c", "f", "a"], [32, 64, 128, 64],
                     ["b", "d", "f"]),
              "2b": (["l", "p", "r"], [512, 4, 512], ["r", "q", "s"], [512, 4, 512], ["l", "p", "q", "s"])}
 

@@ -6,8 +6,8 @@
 // is C's fastest. HBM-bound: algorithmic bytes = numel(C) * (sizeof A +
 // sizeof C) + numel(B) * sizeof B.
 //  * row kernel  — C's fastest mode is long (>= 64): one block walks rows of
-//                  it, so loads and stores of A and C are coalesced (with 64
-//                  bytes of loads in flight per thread when all types agree);
+//                  it, so loads and stores of A and C are coalesced (with four
+//                  loads in flight per thread when all types agree);
 //  * flat kernel — every element decodes its own offsets.
 // Element types: the product is formed in T = promote(A, B) (float, double,
 // float2 or double2) from operands of any narrower type, and stored in C's.
@@ -141,9 +141,9 @@ __global__ void __launch_bounds__(256) k_hadamard_rows(HArgs a, ModeGroup outer,
     }
 }
 
-// Same element type everywhere and A, C unit-stride along the row: 64 bytes
-// of independent loads in flight per thread, and a broadcast B (stride 0
-// along the row) read once per row.
+// Same element type everywhere and A, C unit-stride along the row: four
+// independent loads in flight per thread, and a broadcast B (stride 0 along
+// the row) read once per row.
 // Work items are (row, chunk of HCHUNK elements) so that the grid balances
 // even when the rows are few and long.
 constexpr int64_t HCHUNK = 4096;
@@ -152,7 +152,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_hadamard_rows_same(const T *__restrict__ A, const T *__restrict__ B,
                                                             T *__restrict__ C, ModeGroup outer, int64_t len,
                                                             int64_t sb, int64_t rows) {
-    constexpr int U = 64 / (int)sizeof(T);  // 64 bytes of A in flight per thread
+    constexpr int U = 4;  // measured: 8 in flight per thread was slower for 8-byte types
     const int64_t chunks = (len + HCHUNK - 1) / HCHUNK;
     for (int64_t w = blockIdx.x; w < rows * chunks; w += gridDim.x) {
         const int64_t r = w / chunks, lo = (w - r * chunks) * HCHUNK, hi = min(len, lo + HCHUNK);
