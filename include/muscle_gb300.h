@@ -220,6 +220,13 @@ const char *mgb_last_error(void);
 /* Reads and clears the device-side status word written by bounded waits and
  * non-finite checks of kernels launched on `stream` (synchronises it).     */
 int mgb_device_status(void *stream, int32_t *status);
+/* Self-test of the bounded device waits (no counterpart in the reference):
+ * launches one CTA whose mbarrier wait nothing ever completes, through the
+ * same wait routine the contraction kernels use. The wait gives up after its
+ * limit (about a second), records MGB_ERR_DEVICE_TIMEOUT in the device status
+ * word and the kernel returns normally, so the context stays usable. Read the
+ * word with mgb_device_status afterwards.                                  */
+int mgb_selftest_wait_timeout(void *stream);
 /* Library version string. */
 const char *mgb_version(void);
 

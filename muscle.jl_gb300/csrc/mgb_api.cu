@@ -520,6 +520,8 @@ int mgb_unary(mgb_plan plan, const void *X, void *Y, void *workspace, uint64_t w
     return launch_unary(up, X, Y, (cudaStream_t)stream);
 }
 
+int mgb_selftest_wait_timeout(void *stream) { return selftest_wait_timeout((cudaStream_t)stream); }
+
 int mgb_device_status(void *stream, int32_t *status) {
     if (!status) return fail(MGB_ERR_ARGUMENT, "null status pointer");
     MGB_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));

@@ -149,6 +149,7 @@ int launch_plain_gemm(const ContractionPlan &p, const void *A, const void *B, vo
 int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C,
                  void *ws, cudaStream_t s, cudaEvent_t mid = nullptr);
 int launch_unary(const UnaryPlan &p, const void *X, void *Y, cudaStream_t s);
+int selftest_wait_timeout(cudaStream_t s);
 int launch_hadamard(const ModeGroup &g, int ta, int tb, int tc, const void *A, const void *B, void *C,
                     cudaStream_t s);
 int32_t *device_status_ptr();  // per-device status word

@@ -805,6 +805,32 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 }
 
 // =============================================================================
+// Self-test of the bounded waits: one CTA waits on an mbarrier that nothing
+// completes, with the production wait routine, and must come back with
+// MGB_ERR_DEVICE_TIMEOUT in the status word.
+// =============================================================================
+__global__ void k_wait_selftest(int32_t *status) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&bar), 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) (void)mbar_wait(smem_u32(&bar), 0, &abort_flag, status);
+    __syncthreads();
+}
+
+int selftest_wait_timeout(cudaStream_t s) {
+    int32_t *status = device_status_ptr();
+    if (!status) return fail(MGB_ERR_CUDA, "device status word unavailable");
+    k_wait_selftest<<<1, 32, 0, s>>>(status);
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
+}
+
+// =============================================================================
 // Host side
 // =============================================================================
 static uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }

@@ -105,6 +105,7 @@ SIGNATURES = {
     "mgb_server_destroy": (_i32, [_vp]),
     "mgb_last_error": (ctypes.c_char_p, []),
     "mgb_device_status": (_i32, [_vp, _P(_i32)]),
+    "mgb_selftest_wait_timeout": (_i32, [_vp]),
     "mgb_version": (ctypes.c_char_p, []),
 }
 
