@@ -58,11 +58,11 @@ def parse():
     ap.add_argument("--native-steps", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "peps", "serve", "config2", "kernel", "permute", "hadamard"],
+                    choices=["precision", "peps", "serve", "config2", "kernel", "permute", "hadamard", "unary"],
                     help="precision: the headline line; peps / serve: batching and serving forms; config2: "
                          "plain shapes that permute; kernel / permute: one contraction of the precision "
                          "workload at --n / the permutation of A(a,b,c,d,e) with e = --perm-e (profiling cases); "
-                         "hadamard: broadcast product of a 4.3 GB array")
+                         "hadamard / unary: broadcast product / partial sums of a 4.3 GB array")
     ap.add_argument("--form", default="ozaki", help="form of --workload kernel")
     ap.add_argument("--perm-e", type=int, default=32, help="extent of label e in --workload permute")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="per offered rate in the serving sweep")
@@ -581,6 +581,42 @@ def hadamard_case(dev, steps, warmup):
     return out
 
 
+def unary_case(dev, steps, warmup):
+    """unary_einsum partial sums of a ComplexF64 X(a,b,c) = 4096 x 1024 x 64
+    (4.3 GB): over the middle label b (a thread per output, coalesced over a)
+    and over the contiguous label a (a warp per output). HBM-bound: algorithmic
+    bytes = read X + write Y."""
+    import torch
+
+    import muscle_gb300 as m
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    ea = [4096, 1024, 64]
+    x = torch.randn(list(reversed(ea)), dtype=torch.complex128, device=dev, generator=g).permute(2, 1, 0)
+    X = m.Tensor(x, ["a", "b", "c"])
+    _, hbm, kind = peaks()
+    out = {}
+    for name, keep, dim in (("sum_over_b", ["a", "c"], 1), ("sum_over_a", ["b", "c"], 0)):
+        Y = m.Tensor(m.empty_colmajor([ea[["a", "b", "c"].index(i)] for i in keep], torch.complex128, dev), keep)
+        for _ in range(warmup):
+            m.unary_einsum_(Y, X)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            m.unary_einsum_(Y, X)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        nb = (x.numel() + Y.data.numel()) * 16
+        want = x.sum(dim=dim)
+        ok = bool((Y.data - want).abs().max().item() <= 1e-12 * want.abs().max().item())
+        out[name] = {"bytes": nb, "ms": ms, "gbs": nb / (ms / 1e3) / 1e9, "frac_of_hbm": nb / (ms / 1e3) / 1e9 / hbm,
+                     "peak_kind": kind, "matches_torch": ok}
+    return out
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -626,6 +662,9 @@ def main():
         elif args.workload == "permute":
             res = permute_case(dev, args.perm_e, args.steps, args.warmup)
             metric = "permutation kernel GB/s (profiling case)"
+        elif args.workload == "unary":
+            res = unary_case(dev, args.steps, args.warmup)
+            metric = "unary_einsum partial sums GB/s"
         elif args.workload == "hadamard":
             res = hadamard_case(dev, args.steps, args.warmup)
             metric = "hadamard (broadcast product) GB/s"

@@ -53,15 +53,28 @@ __device__ __forceinline__ double2 shfl_down(double2 v, int d) {
     return make_double2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
 }
 
-// One thread per output (short reductions).
+// One thread per output: consecutive threads take consecutive outputs, so
+// the loads are coalesced when Y's fastest mode is also X's (a sum over a
+// slower label); the fastest reduced mode is walked without division.
 template <typename T>
 __global__ void k_unary_thread(const T *__restrict__ x, T *__restrict__ y, ModeGroup go, ModeGroup gr,
                                int64_t O, int64_t R) {
+    const int64_t e0 = gr.ext[0], s0 = gr.str[0][0];
+    ModeGroup rest = gr;
+    rest.n = gr.n - 1;
+    for (int i = 0; i < rest.n; ++i) {
+        rest.ext[i] = gr.ext[i + 1];
+        rest.str[0][i] = gr.str[0][i + 1];
+    }
+    const int64_t outer = R / e0;
     for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < O;
          o += (int64_t)gridDim.x * blockDim.x) {
         const T *xo = x + group_offset(go, 0, o);
         T acc = Acc<T>::zero();
-        for (int64_t r = 0; r < R; ++r) acc = Acc<T>::add(acc, xo[group_offset(gr, 0, r)]);
+        for (int64_t q = 0; q < outer; ++q) {
+            const T *xq = xo + group_offset(rest, 0, q);
+            for (int64_t r = 0; r < e0; ++r) acc = Acc<T>::add(acc, __ldg(xq + r * s0));
+        }
         y[group_offset(go, 1, o)] = acc;
     }
 }
@@ -87,7 +100,7 @@ __global__ void k_unary_warp(const T *__restrict__ x, T *__restrict__ y, ModeGro
         T acc = Acc<T>::zero();
         for (int64_t q = 0; q < outer; ++q) {
             const T *xq = xo + group_offset(rest, 0, q);
-            for (int64_t r = lane; r < e0; r += 32) acc = Acc<T>::add(acc, xq[r * s0]);
+            for (int64_t r = lane; r < e0; r += 32) acc = Acc<T>::add(acc, __ldg(xq + r * s0));
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) acc = Acc<T>::add(acc, shfl_down(acc, d));
@@ -108,7 +121,12 @@ static int run_unary(const UnaryPlan &p, const T *x, T *y, cudaStream_t s) {
         gr.ext[0] = 1;
         gr.str[0][0] = gr.str[1][0] = gr.str[2][0] = 0;
     }
-    if (p.R >= 64) {
+    // a warp per output when the reduction runs along X's contiguous mode (or
+    // no mode of the output is contiguous in X and the reduction is long);
+    // otherwise a thread per output, coalesced over the outputs
+    const bool red_contig = std::llabs(gr.str[0][0]) == 1 && gr.ext[0] > 1;
+    const bool out_contig = std::llabs(go.str[0][0]) == 1 && go.ext[0] > 1;
+    if (p.R >= 64 && (red_contig || !out_contig)) {
         int64_t blocks = std::min<int64_t>((p.O * 32 + 255) / 256, 152 * 16);
         k_unary_warp<T><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(x, y, go, gr, p.O, p.R);
     } else {
