@@ -163,7 +163,8 @@ int mgb_group_execute_part(mgb_group group, int32_t part, int32_t nparts,
 /* Tile schedule of the batched tensor-core launches: per member, an index
  * 0..5 into the rasterisation bands {1, 2, 3, 4, 8, 16} (row tiles walked
  * together across all column tiles); a bucket takes its first member's
- * value; -1 = default band (16). Written by the host-side autotuner.      */
+ * value; any other index = the library's default band (3). Written by the
+ * host-side autotuner.                                                    */
 int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan);
 int mgb_group_destroy(mgb_group group);
 

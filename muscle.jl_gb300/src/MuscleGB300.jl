@@ -2,13 +2,15 @@
     MuscleGB300
 
 A Muscle.jl backend for device-resident tensors on NVIDIA GB300 (sm_103a).
-Loading this package registers `BackendGB300` as the backend for
-`binary_einsum`, `binary_einsum!`, `unary_einsum` and `unary_einsum!` on
-`(DomainCUDA, ...)` operands (the rule tables of
-src/Operations/binary_einsum.jl:20-31 and src/Operations/unary_einsum.jl:20-24),
-and implements those operations by `ccall` into `libmuscle_gb300.so`
-(C ABI in include/muscle_gb300.h). `with_backend(f, BackendGB300(...))`
-selects a form explicitly.
+`enable!()` registers `BackendGB300` as the backend for `binary_einsum`,
+`binary_einsum!`, `unary_einsum`, `unary_einsum!`, `hadamard` and `hadamard!`
+on `(DomainCUDA, ...)` operands (the rule tables of
+src/Operations/binary_einsum.jl:20-31, src/Operations/unary_einsum.jl:20-24
+and src/Operations/hadamard.jl:4-5); the methods `ccall` into
+`libmuscle_gb300.so` (C ABI in include/muscle_gb300.h).
+`with_backend(f, BackendGB300(...))` selects a form explicitly. `Server` is
+the serving loop: contractions submitted as they arrive, admitted against a
+device-memory budget and batched onto several streams.
 """
 module MuscleGB300
 
@@ -16,7 +18,7 @@ using CUDA
 using Muscle
 using Muscle: Backend, DomainCUDA, Index, Tensor, inds
 
-export BackendGB300
+export BackendGB300, Server, submit!
 
 const libmgb = get(ENV, "MUSCLE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libmuscle_gb300.so"))
 
@@ -164,6 +166,72 @@ function Muscle.hadamard!(be::BackendGB300, c::Tensor, a::Tensor, b::Tensor)
                     da, db, dc, parent(a), parent(b), parent(c), CUDA.stream()))
     end
     return c
+end
+
+# ---------------------------------------------------------------------------
+# Serving loop (mgb_server_*): contractions submitted as they arrive, admitted
+# against a device-memory byte budget and batched onto several streams by the
+# library's scheduler thread.
+
+"""
+    Server(budget_bytes; streams=4, max_batch=256)
+
+A request loop on the current device. `submit!` hands it a contraction
+`c = a * b` (labels as in `binary_einsum!`); `wait` blocks for its result.
+The tensors must stay alive until `wait` returns for their ticket.
+"""
+mutable struct Server
+    handle::Ptr{Cvoid}
+    plans::Dict{Int64,Ptr{Cvoid}}  # ticket -> plan, destroyed once waited for
+end
+
+function Server(budget_bytes::Integer; streams::Integer=4, max_batch::Integer=256)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:mgb_server_create, libmgb), Cint, (Ptr{Ptr{Cvoid}}, UInt64, Cint, Cint),
+                h, UInt64(budget_bytes), Cint(streams), Cint(max_batch)))
+    srv = Server(h[], Dict{Int64,Ptr{Cvoid}}())
+    finalizer(close, srv)
+    return srv
+end
+
+function submit!(srv::Server, c::Tensor, a::Tensor, b::Tensor; backend::BackendGB300=BackendGB300())
+    m = modemap(a, b, c)
+    aa, ab, ac = descarrays(a, m), descarrays(b, m), descarrays(c, m)
+    plan = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve aa ab ac begin
+        da, db, dc = Ref(desc(a, aa)), Ref(desc(b, ab)), Ref(desc(c, ac))
+        check(ccall((:mgb_contraction_plan, libmgb), Cint,
+                    (Ptr{Ptr{Cvoid}}, Ref{TensorDesc}, Ref{TensorDesc}, Ref{TensorDesc}, Cint, Cint),
+                    plan, da, db, dc, backend.form, backend.slices))
+    end
+    resident = UInt64(sizeof(parent(a)) + sizeof(parent(b)) + sizeof(parent(c)))
+    ticket = Ref{Int64}(0)
+    check(ccall((:mgb_server_submit, libmgb), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, UInt64, CUDA.CUstream, Ref{Int64}),
+                srv.handle, plan[], parent(a), parent(b), parent(c), resident, CUDA.stream(), ticket))
+    srv.plans[ticket[]] = plan[]
+    return ticket[]
+end
+
+function Base.wait(srv::Server, ticket::Integer; timeout::Real=-1)
+    status = Ref{Cint}(0)
+    check(ccall((:mgb_server_wait, libmgb), Cint, (Ptr{Cvoid}, Int64, Cdouble, Ref{Cint}),
+                srv.handle, Int64(ticket), Cdouble(timeout), status))
+    plan = pop!(srv.plans, Int64(ticket), C_NULL)
+    plan == C_NULL || ccall((:mgb_plan_destroy, libmgb), Cint, (Ptr{Cvoid},), plan)
+    check(status[])
+    return nothing
+end
+
+function Base.close(srv::Server)
+    srv.handle == C_NULL && return nothing
+    ccall((:mgb_server_destroy, libmgb), Cint, (Ptr{Cvoid},), srv.handle)
+    for plan in values(srv.plans)
+        ccall((:mgb_plan_destroy, libmgb), Cint, (Ptr{Cvoid},), plan)
+    end
+    empty!(srv.plans)
+    srv.handle = C_NULL
+    return nothing
 end
 
 """
