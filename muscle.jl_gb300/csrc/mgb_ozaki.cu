@@ -33,16 +33,20 @@
 // B_e[2n+q][2k+p] holds [[Br, -Bi], [Bi, Br]] so that C_e[m][2n+q] is part q
 // of C[m,n] (4 real products per complex product, as zgemm's 4M form).
 //
-// Pipeline per CTA (128 x 32 embedded outputs, one CTA per SM):
+// Pipeline per CTA (128 x BN embedded outputs, BN = 32, or 64 for S = 3;
+// one CTA per SM):
 //   warp 0       TMA producer: one 3-D box per operand per 32-wide k block
 //                loads all S slices at once into a 64B-swizzled stage;
-//   warp 1       TMEM allocation, then a single thread issues, per 16 k,
-//                one tcgen05.mma.cta_group::1.kind::f16 per A slice i with
-//                M = 128, N = 32 (S - i): B slices 0 .. S-1-i lie back to
+//   warp 1       TMEM allocation, then one thread issues, per 16 k, one
+//                tcgen05.mma.cta_group::1.kind::f16 per A slice i with
+//                M = 128, N = BN (S - i): B slices 0 .. S-1-i lie back to
 //                back in the stage and their accumulators (digit groups
 //                i .. S-1) lie back to back in TMEM;
-//   warps 2..9   epilogue: tcgen05.ld 32x32b.x16 per group and column half,
-//                from the bank the MMAs are not writing.
+//   warp 10      (OZAKI) a second issuing thread: the two take alternate
+//                k blocks;
+//   warps 2..9   epilogue: tcgen05.ld 32x32b.x16 per group and column half
+//                from the bank the MMAs are not writing, then tcgen05.st of
+//                zeros into what was read.
 // Every mbarrier wait is bounded; on timeout the CTA records
 // MGB_ERR_DEVICE_TIMEOUT in the device status word, drains its copies and
 // MMAs, frees TMEM and returns.
