@@ -345,8 +345,10 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
         g = tuner.group(items)
         flops = g.flops
         by_parts = {}
-        for parts in (1, 4):
-            graph = g.capture(parts)
+        # (branches, persistent): one persistent tensor-core launch per kernel
+        # variant after the pre-passes, or every bucket's own launches
+        for parts, pers in ((1, True), (4, True), (4, False)):
+            graph = g.capture(parts, pers)
             for _ in range(3):
                 graph.replay()
             torch.cuda.synchronize(dev)
@@ -356,7 +358,7 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
                 graph.replay()
             e1.record()
             torch.cuda.synchronize(dev)
-            by_parts[parts] = e0.elapsed_time(e1) / steps
+            by_parts[(parts, pers)] = e0.elapsed_time(e1) / steps
             del graph
         best_parts = min(by_parts, key=by_parts.get)
         ms = by_parts[best_parts]
@@ -373,8 +375,8 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
         for f in g.forms:
             forms[f] = forms.get(f, 0) + 1
         key = "c64" if tdt == torch.complex128 else "c32"
-        out[key] = {"graph_ms": ms, "graph_branches": best_parts,
-                    "graph_ms_by_branches": {str(k): v for k, v in by_parts.items()},
+        out[key] = {"graph_ms": ms, "graph_branches": best_parts[0], "persistent": best_parts[1],
+                    "graph_ms_by_branches": {f"{k[0]}{'p' if k[1] else ''}": v for k, v in by_parts.items()},
                     "tflops": flops / (ms / 1e3) / 1e12, "contractions_per_s": len(items) / (ms / 1e3),
                     "one_at_a_time_plain_per_s": one, "forms_chosen": forms, "gflop": flops / 1e9,
                     "distinct_plans": len({id(p) for p in g.plans})}

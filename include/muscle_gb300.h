@@ -150,8 +150,26 @@ int mgb_group_create(mgb_group *group, const mgb_plan *plans, int32_t count,
 int mgb_group_update(mgb_group group, const void *const *A,
                      const void *const *B, void *const *C);
 int mgb_group_workspace_size(mgb_group group, uint64_t *bytes);
+/* Runs every member on `stream`: the pre-passes of the emulated buckets and
+ * the plain buckets, then ONE persistent tensor-core launch per kernel
+ * variant over all emulated buckets (each CTA walks tiles of every bucket),
+ * then members that run alone. The first execution with a given workspace
+ * (and the first after mgb_group_set_tiles) uploads the persistent launch's
+ * job table with a synchronous copy; capture the group in a CUDA graph after
+ * such a warm-up execution.                                                */
 int mgb_group_execute(mgb_group group, void *workspace,
                       uint64_t workspace_bytes, void *stream);
+/* mgb_group_execute in two steps, so that the first can run on several
+ * streams: mgb_group_prepare_part runs the pre-passes of the emulated
+ * buckets and the plain buckets of part `part` of `nparts` (dealt as in
+ * mgb_group_execute_part); once every part has finished, mgb_group_finish
+ * runs the persistent tensor-core launches and the members that run alone.
+ * No counterpart in the reference.                                        */
+int mgb_group_prepare_part(mgb_group group, int32_t part, int32_t nparts,
+                           void *workspace, uint64_t workspace_bytes,
+                           void *stream);
+int mgb_group_finish(mgb_group group, void *workspace,
+                     uint64_t workspace_bytes, void *stream);
 /* The members of part `part` of `nparts` (0 <= part < nparts). The work units
  * (batched buckets and single members) are dealt, largest first, to the part
  * with the least work so far. Parts touch disjoint outputs and workspace

@@ -13,6 +13,7 @@
 // per-member slices.
 #include <algorithm>
 #include <map>
+#include <tuple>
 #include <vector>
 
 #include "mgb_internal.h"
@@ -43,6 +44,12 @@ struct mgb_group_s {
     std::vector<Bucket> buckets;
     std::vector<Single> singles;
     uint64_t ws_bytes = 0;
+    // One persistent GEMM launch per kernel variant of the emulated buckets;
+    // its job table holds slice addresses inside the workspace, so it is
+    // built on the first execution with a workspace and rebuilt when the
+    // workspace moves.
+    void *grouped_ws = nullptr;
+    std::vector<mgb::OzGrouped *> grouped;
 };
 
 using namespace mgb;
@@ -69,10 +76,40 @@ static int upload(mgb_group g) {
     return MGB_OK;
 }
 
+static void free_grouped(mgb_group g) {
+    for (auto *x : g->grouped) ozaki_grouped_destroy(x);
+    g->grouped.clear();
+    g->grouped_ws = nullptr;
+}
+
 static void free_group(mgb_group g) {
+    free_grouped(g);
     for (auto &b : g->buckets)
         if (b.dptr) cudaFree(b.dptr);
     delete g;
+}
+
+// Job tables of the persistent GEMM launches, one per kernel variant
+// (slices, form, real or complex) of the emulated buckets.
+static int build_grouped(mgb_group g, void *workspace) {
+    free_grouped(g);
+    std::map<std::tuple<int, int, int>, std::pair<std::vector<const ContractionPlan *>, std::vector<void *>>> sets;
+    for (auto &b : g->buckets) {
+        if (b.cp.form == MGB_FORM_PLAIN) continue;
+        auto &e = sets[std::make_tuple(b.cp.slices, b.cp.form, is_complex(b.cp.compute_dtype) ? 1 : 0)];
+        e.first.push_back(&b.cp);
+        e.second.push_back((char *)workspace + b.ws_off);
+    }
+    for (auto &kv : sets) {
+        OzGrouped *x = nullptr;
+        if (int st = ozaki_grouped_create(kv.second.first, kv.second.second, &x)) {
+            free_grouped(g);
+            return st;
+        }
+        g->grouped.push_back(x);
+    }
+    g->grouped_ws = workspace;
+    return MGB_OK;
 }
 
 extern "C" {
@@ -168,6 +205,7 @@ int mgb_group_set_tiles(mgb_group group, const int32_t *tile_per_plan) {
         const int t = tile_per_plan[b.members.front()];
         b.cp.band = (t >= 0 && t < 6) ? kBands[t] : 0;
     }
+    group->grouped_ws = nullptr;  // the job tables embed the bands: rebuild on the next execution
     return MGB_OK;
 }
 
@@ -207,8 +245,55 @@ static int run_unit(mgb_group g, int u, void *workspace, cudaStream_t s) {
     return mgb_contract(p, g->A[m.member], g->B[m.member], g->C[m.member], w, p->cp.ws_bytes, s);
 }
 
+static int check_ws(mgb_group group, void *workspace, uint64_t workspace_bytes) {
+    if (!group) return fail(MGB_ERR_ARGUMENT, "group: null argument");
+    if (workspace_bytes < group->ws_bytes || (group->ws_bytes && !workspace))
+        return fail(MGB_ERR_WORKSPACE, "group workspace smaller than mgb_group_workspace_size");
+    return MGB_OK;
+}
+
+int mgb_group_prepare_part(mgb_group group, int32_t part, int32_t nparts, void *workspace, uint64_t workspace_bytes,
+                           void *stream) {
+    if (int st = check_ws(group, workspace, workspace_bytes)) return st;
+    if (nparts < 1 || part < 0 || part >= nparts) return fail(MGB_ERR_ARGUMENT, "group: part out of range");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nb = (int)group->buckets.size();
+    auto one = [&](int u) -> int {
+        Bucket &b = group->buckets[u];
+        return b.cp.form == MGB_FORM_PLAIN ? launch_plain_gemm(b.cp, nullptr, nullptr, nullptr, s)
+                                           : ozaki_prepass(b.cp, nullptr, nullptr, (char *)workspace + b.ws_off, s);
+    };
+    if (nparts == 1) {
+        for (int u = 0; u < nb; ++u)
+            if (int st = one(u)) return st;
+        return MGB_OK;
+    }
+    for (int u : part_units(group, part, nparts))
+        if (u < nb)
+            if (int st = one(u)) return st;
+    return MGB_OK;
+}
+
+int mgb_group_finish(mgb_group group, void *workspace, uint64_t workspace_bytes, void *stream) {
+    if (int st = check_ws(group, workspace, workspace_bytes)) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (group->grouped_ws != workspace)
+        if (int st = build_grouped(group, workspace)) return st;
+    for (auto *x : group->grouped)
+        if (int st = ozaki_grouped_launch(x, s)) return st;
+    const int nb = (int)group->buckets.size(), nu = nb + (int)group->singles.size();
+    for (int u = nb; u < nu; ++u)
+        if (int st = run_unit(group, u, workspace, s)) return st;
+    return MGB_OK;
+}
+
 int mgb_group_execute(mgb_group group, void *workspace, uint64_t workspace_bytes, void *stream) {
-    return mgb_group_execute_part(group, 0, 1, workspace, workspace_bytes, stream);
+    if (int st = check_ws(group, workspace, workspace_bytes)) return st;
+    // build the job tables before any launch, so that a failure leaves no work queued
+    if (group->grouped_ws != workspace)
+        if (int st = build_grouped(group, workspace)) return st;
+    if (int st = mgb_group_prepare_part(group, 0, 1, workspace, workspace_bytes, stream)) return st;
+    return mgb_group_finish(group, workspace, workspace_bytes, stream);
 }
 
 int mgb_group_execute_part(mgb_group group, int32_t part, int32_t nparts, void *workspace, uint64_t workspace_bytes,

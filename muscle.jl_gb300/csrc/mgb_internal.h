@@ -150,6 +150,15 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
                  void *ws, cudaStream_t s, cudaEvent_t mid = nullptr);
 int launch_unary(const UnaryPlan &p, const void *X, void *Y, cudaStream_t s);
 int selftest_wait_timeout(cudaStream_t s);
+// Emulated forms split for groups: the pre-pass of one plan, and one
+// persistent GEMM launch for several plans of one kernel variant (same
+// slices, form and real/complex) whose slices lie in the given workspaces.
+int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *ws, cudaStream_t s);
+struct OzGrouped;
+int ozaki_grouped_create(const std::vector<const ContractionPlan *> &plans, const std::vector<void *> &ws,
+                         OzGrouped **out);
+int ozaki_grouped_launch(const OzGrouped *g, cudaStream_t s);
+void ozaki_grouped_destroy(OzGrouped *g);
 int launch_hadamard(const ModeGroup &g, int ta, int tb, int tc, const void *A, const void *B, void *C,
                     cudaStream_t s);
 int32_t *device_status_ptr();  // per-device status word

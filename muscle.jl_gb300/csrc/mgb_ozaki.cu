@@ -54,8 +54,10 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <mutex>
+#include <vector>
 
 #include "mgb_internal.h"
 
@@ -500,7 +502,62 @@ struct OzGemmArgs {
     int32_t *status;
 };
 
-// One CTA computes a 128 x BN tile of the embedded output. Digit group
+// One contraction (or one bucket of a group) as the GEMM sees it: the slice
+// tensor maps, the arguments and its tile grid (column tiles x row tiles x
+// batch entries).
+struct alignas(64) OzJob {
+    CUtensorMap tmA, tmB;
+    OzGemmArgs a;
+    int32_t tiles_n, tiles_m, L;
+};
+
+// Tile sources of the kernel: one job in the parameter space, or a table of
+// jobs in global memory (a group) whose tiles are numbered consecutively.
+struct OzOneJob {
+    const OzJob *j;
+    __device__ int64_t tiles() const { return (int64_t)j->tiles_n * j->tiles_m * j->L; }
+    __device__ const OzJob &job(int64_t t, int64_t &local) const {
+        local = t;
+        return *j;
+    }
+};
+struct OzJobTable {
+    const OzJob *jobs;
+    const int64_t *start;  // [n + 1]: first tile of each job, then the total
+    int n;
+    __device__ int64_t tiles() const { return start[n]; }
+    __device__ const OzJob &job(int64_t t, int64_t &local) const {
+        int lo = 0, hi = n - 1;  // the last job with start <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (start[mid] <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        local = t - start[lo];
+        return jobs[lo];
+    }
+};
+
+// Tile `local` of a job: batch entry, then grouped rasterisation within the
+// entry, so that consecutive tiles walk a band of `band` row tiles across all
+// column tiles and the CTAs resident at the same time share slices in L2.
+__device__ __forceinline__ void oz_tile(const OzJob &J, int64_t local, int bn, int64_t &m0, int64_t &n0, int &l) {
+    const int64_t nn = J.tiles_n, nm = J.tiles_m, per = nn * nm;
+    l = (int)(local / per);
+    const int64_t t = local - (int64_t)l * per;
+    const int64_t gm = J.a.band;
+    const int64_t band = t / (gm * nn);
+    const int64_t first = band * gm;
+    const int64_t rows = min(gm, nm - first);
+    const int64_t r = t - band * gm * nn;
+    m0 = (first + r % rows) * OZ_BM;
+    n0 = (r / rows) * bn;
+}
+
+// One CTA computes 128 x BN tiles of the embedded output, in turn for the
+// tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...: the stage ring, the
+// TMEM banks and their barriers run on across tiles, so the loads of the
+// next tile overlap the MMAs and the readout of the current one. Digit group
 // g = i + j (0-based slice indices of A and B) owns BN TMEM columns; the S
 // groups of a chunk form one bank of BN S columns, and two banks alternate
 // so that the epilogue reads chunk c while the MMAs fill chunk c + 1.
@@ -511,10 +568,8 @@ struct OzGemmArgs {
 // is read from shared memory once per 16 k. BN = 64 for S = 3 (BF16X3
 // included) and 32 for S >= 4: the widest that two banks leave room for
 // while the epilogue's 96-bit accumulators stay in registers.
-template <int S, bool EXACT, bool CX>
-__global__ void __launch_bounds__(OZ_THREADS, 1)
-    k_oz_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-              const OzGemmArgs args) {
+template <int S, bool EXACT, bool CX, typename Src>
+__device__ __forceinline__ void oz_gemm_body(const Src &src) {
     constexpr int W = oz_digit_bits(S);  // digit width (EXACT)
     constexpr int NST = oz_stages(S);
     constexpr int STAGE = oz_stage_bytes(S);
@@ -546,37 +601,27 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     uint32_t *tmem_slot = (uint32_t *)(done + 2);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
-    // Stage-landed barriers. Each one is waited on by a single issuer and in
+    // Stage-landed barriers, indexed by the CTA's running k-block count g
+    // (across its tiles). Each barrier is waited on by a single issuer and in
     // order of its phases: an mbarrier parity wait cannot tell phase r from
     // phase r - 2, so a waiter that could run two phases ahead of a barrier
     // would pass early. With two issuers and an odd stage count the rounds of
     // a stage alternate between the issuers, so every stage gets one barrier
-    // per issuer (index 2 s + kb % 2) and each of those is used every other
+    // per issuer (index 2 s + g % 2) and each of those is used every other
     // round; otherwise stage s always has the same issuer (index 2 s + s % 2,
     // or 2 s for one issuer), used every round.
-    auto full_idx = [](int kb) { return 2 * (kb % NST) + (NI == 2 ? (kb & 1) : 0); };
-    auto full_par = [](int kb) {
-        const uint32_t r = (uint32_t)(kb / NST);
+    auto full_idx = [](uint32_t g) { return 2 * (int)(g % NST) + (NI == 2 ? (int)(g & 1u) : 0); };
+    auto full_par = [](uint32_t g) {
+        const uint32_t r = g / NST;
         return (NI == 2 && (NST & 1)) ? (r >> 1) & 1u : r & 1u;
     };
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    // Grouped rasterisation: consecutive CTAs walk a band of `band` row tiles
-    // across all column tiles, so the slices of A and B they read are shared
-    // in L2 by the CTAs resident at the same time.
-    int64_t m_tile, n_tile;
+    const int64_t T = src.tiles();
+    int32_t *status;
     {
-        const int64_t nm = gridDim.y, nn = gridDim.x;
-        const int64_t t = (int64_t)blockIdx.y * nn + blockIdx.x;
-        const int64_t gm = args.band;
-        const int64_t band = t / (gm * nn);
-        const int64_t first = band * gm;
-        const int64_t rows = min(gm, nm - first);
-        const int64_t r = t - band * gm * nn;
-        m_tile = first + r % rows;
-        n_tile = r / rows;
+        int64_t unused;
+        status = src.job(0, unused).a.status;
     }
-    const int64_t n0 = n_tile * BN, m0 = m_tile * OZ_BM;
-    const int l = blockIdx.z;
 
     if (tid == 0) {
         for (int s = 0; s < NST; ++s) {
@@ -604,8 +649,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int nkb = args.nkb, kcb = args.kcb;
-    const int nchunks = (nkb + kcb - 1) / kcb;
     // Every MMA accumulates (the issuers' order within a bank is free); the
     // epilogue warps clear both banks here and each bank again after reading it.
     if (warp >= 2 && warp < 2 + OZ_EPI_WARPS) {
@@ -620,58 +663,78 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (warp == 0) {
         // ---------------- TMA producer ----------------
         if (lane == 0) {
-            int issued = 0;
-            for (int kb = 0; kb < nkb; ++kb) {
-                int s = kb % NST;
-                uint32_t round = kb / NST;
-                if (!mbar_wait(smem_u32(empty + s), (round & 1) ^ 1, abort_flag, args.status)) break;
-                uint8_t *st = smem + s * STAGE;
-                const uint32_t fb = smem_u32(full + full_idx(kb));
-                mbar_expect_tx(fb, STAGE);
-                tma_load_3d(smem_u32(st), &tmA, kb * OZ_BK, (int)m0, l * S, fb);
-                tma_load_3d(smem_u32(st + S * OZ_A_TILE), &tmB, kb * OZ_BK, (int)n0, l * S, fb);
-                issued = kb + 1;
-            }
-            // make sure no bulk copy is still writing into shared memory
-            for (int kb = max(0, issued - NST); kb < issued; ++kb)
-                mbar_drain(smem_u32(full + full_idx(kb)), full_par(kb));
-        }
-    } else if (warp == 1 || (NI == 2 && warp == OZ_ISSUER2_WARP)) {
-        // ---------------- MMA issuers ----------------
-        // Issuer `me` takes the k blocks kb with kb % NI == me (kcb is even).
-        // Per chunk c it waits until the epilogue has read and cleared the
-        // bank's previous chunk (c - 2), issues its k blocks, and commits the
-        // chunk's acc_full barrier once (also when it owns no k block of it).
-        if (lane == 0) {
-            const int me = warp == 1 ? 0 : 1;
+            uint32_t g = 0;  // k blocks issued so far, over all tiles of this CTA
             bool ok = true;
-            for (int c = 0; c < nchunks && ok; ++c) {
-                const uint32_t bank = (uint32_t)c & 1u;
-                if (!mbar_wait(smem_u32(acc_empty + bank), ((uint32_t)(c >> 1) & 1u) ^ 1u, abort_flag, args.status)) {
-                    ok = false;
-                    break;
-                }
-                const int kb1 = min(nkb, (c + 1) * kcb);
-                for (int kb = c * kcb + me; kb < kb1; kb += NI) {
-                    const int s = kb % NST;
-                    if (!mbar_wait(smem_u32(full + full_idx(kb)), full_par(kb), abort_flag, args.status)) {
+            for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
+                int64_t local;
+                const OzJob &J = src.job(t, local);
+                int64_t m0, n0;
+                int l;
+                oz_tile(J, local, BN, m0, n0, l);
+                for (int kb = 0; kb < J.a.nkb; ++kb, ++g) {
+                    const int s = (int)(g % NST);
+                    const uint32_t round = g / NST;
+                    if (!mbar_wait(smem_u32(empty + s), (round & 1) ^ 1, abort_flag, status)) {
                         ok = false;
                         break;
                     }
-                    tc_fence_after();
-                    const uint32_t a_base = smem_u32(smem + s * STAGE);
-                    const uint64_t ad0 = sw64_desc(a_base);
-                    const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
-                    const uint32_t d0 = tmem + bank * BANK;
-#pragma unroll
-                    for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
-#pragma unroll
-                        for (int i = 0; i < S; ++i)
-                            tc_mma(d0 + BN * i, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
-                                   bd0 + (uint64_t)((k16 * 32) >> 4), oz_idesc(BN * (S - i)), 1u);
-                    tc_commit(smem_u32(empty + s));
+                    uint8_t *st = smem + s * STAGE;
+                    const uint32_t fb = smem_u32(full + full_idx(g));
+                    mbar_expect_tx(fb, STAGE);
+                    tma_load_3d(smem_u32(st), &J.tmA, kb * OZ_BK, (int)m0, l * S, fb);
+                    tma_load_3d(smem_u32(st + S * OZ_A_TILE), &J.tmB, kb * OZ_BK, (int)n0, l * S, fb);
                 }
-                if (ok) tc_commit(smem_u32(acc_full + bank));
+            }
+            // make sure no bulk copy is still writing into shared memory
+            for (uint32_t gg = g > (uint32_t)NST ? g - NST : 0u; gg < g; ++gg)
+                mbar_drain(smem_u32(full + full_idx(gg)), full_par(gg));
+        }
+    } else if (warp == 1 || (NI == 2 && warp == OZ_ISSUER2_WARP)) {
+        // ---------------- MMA issuers ----------------
+        // Issuer `me` takes the k blocks whose running count g has g % NI == me.
+        // Per chunk C (counted over all tiles) it waits until the epilogue has
+        // read and cleared the bank's previous chunk (C - 2), issues its k
+        // blocks, and commits the chunk's acc_full barrier once (also when it
+        // owns no k block of it).
+        if (lane == 0) {
+            const int me = warp == 1 ? 0 : 1;
+            bool ok = true;
+            uint32_t g = 0, C = 0;
+            for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
+                int64_t local;
+                const OzJob &J = src.job(t, local);
+                const int nkb = J.a.nkb, kcb = J.a.kcb;
+                for (int c0 = 0; c0 < nkb && ok; c0 += kcb, ++C) {
+                    const uint32_t bank = C & 1u;
+                    if (!mbar_wait(smem_u32(acc_empty + bank), ((C >> 1) & 1u) ^ 1u, abort_flag, status)) {
+                        ok = false;
+                        break;
+                    }
+                    const int c1 = min(nkb, c0 + kcb);
+                    for (int kb = c0; kb < c1; ++kb) {
+                        const uint32_t gg = g + (uint32_t)kb;
+                        if (NI == 2 && (int)(gg & 1u) != me) continue;
+                        const int s = (int)(gg % NST);
+                        if (!mbar_wait(smem_u32(full + full_idx(gg)), full_par(gg), abort_flag, status)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t a_base = smem_u32(smem + s * STAGE);
+                        const uint64_t ad0 = sw64_desc(a_base);
+                        const uint64_t bd0 = sw64_desc(a_base + S * OZ_A_TILE);
+                        const uint32_t d0 = tmem + bank * BANK;
+#pragma unroll
+                        for (int k16 = 0; k16 < OZ_BK / 16; ++k16)
+#pragma unroll
+                            for (int i = 0; i < S; ++i)
+                                tc_mma(d0 + BN * i, ad0 + (uint64_t)((i * OZ_A_TILE + k16 * 32) >> 4),
+                                       bd0 + (uint64_t)((k16 * 32) >> 4), oz_idesc(BN * (S - i)), 1u);
+                        tc_commit(smem_u32(empty + s));
+                    }
+                    if (ok) tc_commit(smem_u32(acc_full + bank));
+                }
+                g += (uint32_t)nkb;
             }
             // wait for every MMA this thread issued before TMEM is released
             tc_commit(smem_u32(done + me));
@@ -681,120 +744,131 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         // ---------------- epilogue ----------------
         const int q = warp % 4;        // TMEM lane quarter this warp may access
         const int h = (warp - 2) / 4;  // column half (HALF columns) of each group
-        const int64_t row = m0 + 32 * q + lane;
         const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + HALF * h;
-        // EXACT: one 96-bit two's-complement integer per output column,
-        // X = sum_d G_d 2^(W (S + 1 - d)), held in w0 (bits 0-31), w1, w2.
-        uint32_t w0[EXACT ? HALF : 1], w1[EXACT ? HALF : 1], w2[EXACT ? HALF : 1];
-        // BF16X3: Kahan-compensated float32 sum over the chunks
-        float accf[EXACT ? 1 : HALF], comp[EXACT ? 1 : HALF];
-#pragma unroll
-        for (int j = 0; j < HALF; ++j) {
-            if (EXACT) {
-                w0[j] = 0;
-                w1[j] = 0;
-                w2[j] = 0;
-            } else {
-                accf[j] = 0.f;
-                comp[j] = 0.f;
-            }
-        }
         bool ok = true;
-#pragma unroll 1
-        for (int c = 0; c < nchunks; ++c) {
-            const uint32_t bank = (uint32_t)c & 1u;
-            if (!mbar_wait(smem_u32(acc_full + bank), (uint32_t)(c >> 1) & 1u, abort_flag, args.status)) {
-                ok = false;
-                break;
-            }
-            tc_fence_after();
-            const uint32_t tb = tbase + bank * BANK;
-            if constexpr (EXACT) {
+        uint32_t C = 0;  // chunks read so far, over all tiles of this CTA
+        for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
+            int64_t local;
+            const OzJob &J = src.job(t, local);
+            const OzGemmArgs &args = J.a;
+            int64_t m0, n0;
+            int l;
+            oz_tile(J, local, BN, m0, n0, l);
+            const int64_t row = m0 + 32 * q + lane;
+            const int nchunks = (args.nkb + args.kcb - 1) / args.kcb;
+            // EXACT: one 96-bit two's-complement integer per output column,
+            // X = sum_d G_d 2^(W (S + 1 - d)), held in w0 (bits 0-31), w1, w2.
+            uint32_t w0[EXACT ? HALF : 1], w1[EXACT ? HALF : 1], w2[EXACT ? HALF : 1];
+            // BF16X3: Kahan-compensated float32 sum over the chunks
+            float accf[EXACT ? 1 : HALF], comp[EXACT ? 1 : HALF];
 #pragma unroll
-                for (int g = 0; g < S; ++g) {
-                    uint32_t v[HALF];
-                    tc_ld<HALF>(tb + BN * g, v);
-#pragma unroll
-                    for (int c = 0; c < HALF; c += 16) tc_st16_zero(tb + BN * g + c);
-                    if (g == S - 1) {  // every group of the bank read and cleared
-                        tc_wait_st();
-                        tc_fence_before();
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));
-                    }
-                    const int sh = W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
-                    if (sh < 32) {
-#pragma unroll
-                        for (int j = 0; j < HALF; ++j) {
-                            int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
-                            add96(w0[j], w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32),
-                                  t < 0 ? 0xFFFFFFFFu : 0u);
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < HALF; ++j) {
-                            int64_t t = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
-                            add64hi(w1[j], w2[j], (uint32_t)t, (uint32_t)((uint64_t)t >> 32));
-                        }
-                    }
-                }
-            } else {
-                // pieces hi*hi, then the products of piece-index sum 1 and 2
-                uint32_t v0[HALF], v1[HALF], v2[HALF];
-                tc_ld<HALF>(tb, v0);
-                tc_ld<HALF>(tb + BN, v1);
-                tc_ld<HALF>(tb + 2 * BN, v2);
-#pragma unroll
-                for (int g = 0; g < 3; ++g)
-#pragma unroll
-                    for (int c = 0; c < HALF; c += 16) tc_st16_zero(tb + BN * g + c);
-                tc_wait_st();
-                tc_fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));
-#pragma unroll
-                for (int j = 0; j < HALF; ++j) {
-                    float x = __uint_as_float(v0[j]) + (__uint_as_float(v1[j]) + __uint_as_float(v2[j]));
-                    float y = x - comp[j];
-                    float t = accf[j] + y;
-                    comp[j] = (t - accf[j]) - y;
-                    accf[j] = t;
-                }
-            }
-        }
-        if (ok && row < args.M) {
-            void *const Cl = args.cptr ? args.cptr[l] : args.C;
-            const int64_t lb = args.cptr ? 0 : group_offset(args.gl, 2, l);
-            const int64_t om = group_offset(args.gm, 2, row);
-            int erow = 0;
-            bool badrow = false;
-            if (EXACT) {
-                int be = args.expA[(int64_t)l * args.M + row];
-                badrow = be == 0x7FF;
-                erow = be == 0 ? -1022 : be - 1022;
-            }
-#pragma unroll
-            for (int j = 0; j < HALF; j += (CX ? 2 : 1)) {
-                int64_t ne = n0 + HALF * h + j;
-                if (ne >= args.Ne) continue;
-                int64_t n = CX ? (ne >> 1) : ne;
-                int64_t off = lb + om + group_offset(args.gn, 2, n);
+            for (int j = 0; j < HALF; ++j) {
                 if (EXACT) {
-                    int bc = args.expB[(int64_t)l * args.N + n];
-                    bool bad = badrow || bc == 0x7FF;
-                    int ecol = bc == 0 ? -1022 : bc - 1022;
-                    const int E = erow + ecol - W * (S + 1);
-                    const double nan = __longlong_as_double(0x7FF8000000000000LL);
-                    double v0 = bad ? nan : ldexp(x96_to_double(w0[j], w1[j], w2[j]), E);
-                    if (CX) {
-                        double v1 = bad ? nan : ldexp(x96_to_double(w0[j + 1], w1[j + 1], w2[j + 1]), E);
-                        ((double2 *)Cl)[off] = make_double2(v0, v1);
-                    } else {
-                        ((double *)Cl)[off] = v0;
+                    w0[j] = 0;
+                    w1[j] = 0;
+                    w2[j] = 0;
+                } else {
+                    accf[j] = 0.f;
+                    comp[j] = 0.f;
+                }
+            }
+#pragma unroll 1
+            for (int c = 0; c < nchunks; ++c, ++C) {
+                const uint32_t bank = C & 1u;
+                if (!mbar_wait(smem_u32(acc_full + bank), (C >> 1) & 1u, abort_flag, status)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t tb = tbase + bank * BANK;
+                if constexpr (EXACT) {
+#pragma unroll
+                    for (int g = 0; g < S; ++g) {
+                        uint32_t v[HALF];
+                        tc_ld<HALF>(tb + BN * g, v);
+#pragma unroll
+                        for (int c2 = 0; c2 < HALF; c2 += 16) tc_st16_zero(tb + BN * g + c2);
+                        if (g == S - 1) {  // every group of the bank read and cleared
+                            tc_wait_st();
+                            tc_fence_before();
+                            __syncwarp();
+                            if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));
+                        }
+                        const int sh = W * (S - 1 - g);  // W (S + 1 - d), d = g + 2
+                        if (sh < 32) {
+#pragma unroll
+                            for (int j = 0; j < HALF; ++j) {
+                                int64_t x = (int64_t)__float2int_rn(__uint_as_float(v[j])) << sh;
+                                add96(w0[j], w1[j], w2[j], (uint32_t)x, (uint32_t)((uint64_t)x >> 32),
+                                      x < 0 ? 0xFFFFFFFFu : 0u);
+                            }
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < HALF; ++j) {
+                                int64_t x = (int64_t)__float2int_rn(__uint_as_float(v[j])) << (sh - 32);
+                                add64hi(w1[j], w2[j], (uint32_t)x, (uint32_t)((uint64_t)x >> 32));
+                            }
+                        }
                     }
                 } else {
-                    if (CX) ((float2 *)Cl)[off] = make_float2(accf[j], accf[j + 1]);
-                    else ((float *)Cl)[off] = accf[j];
+                    // pieces hi*hi, then the products of piece-index sum 1 and 2
+                    uint32_t v0[HALF], v1[HALF], v2[HALF];
+                    tc_ld<HALF>(tb, v0);
+                    tc_ld<HALF>(tb + BN, v1);
+                    tc_ld<HALF>(tb + 2 * BN, v2);
+#pragma unroll
+                    for (int g = 0; g < 3; ++g)
+#pragma unroll
+                        for (int c2 = 0; c2 < HALF; c2 += 16) tc_st16_zero(tb + BN * g + c2);
+                    tc_wait_st();
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));
+#pragma unroll
+                    for (int j = 0; j < HALF; ++j) {
+                        float x = __uint_as_float(v0[j]) + (__uint_as_float(v1[j]) + __uint_as_float(v2[j]));
+                        float y = x - comp[j];
+                        float s2 = accf[j] + y;
+                        comp[j] = (s2 - accf[j]) - y;
+                        accf[j] = s2;
+                    }
+                }
+            }
+            if (!ok) break;
+            if (row < args.M) {
+                void *const Cl = args.cptr ? args.cptr[l] : args.C;
+                const int64_t lb = args.cptr ? 0 : group_offset(args.gl, 2, l);
+                const int64_t om = group_offset(args.gm, 2, row);
+                int erow = 0;
+                bool badrow = false;
+                if (EXACT) {
+                    int be = args.expA[(int64_t)l * args.M + row];
+                    badrow = be == 0x7FF;
+                    erow = be == 0 ? -1022 : be - 1022;
+                }
+#pragma unroll
+                for (int j = 0; j < HALF; j += (CX ? 2 : 1)) {
+                    int64_t ne = n0 + HALF * h + j;
+                    if (ne >= args.Ne) continue;
+                    int64_t n = CX ? (ne >> 1) : ne;
+                    int64_t off = lb + om + group_offset(args.gn, 2, n);
+                    if (EXACT) {
+                        int bc = args.expB[(int64_t)l * args.N + n];
+                        bool bad = badrow || bc == 0x7FF;
+                        int ecol = bc == 0 ? -1022 : bc - 1022;
+                        const int E = erow + ecol - W * (S + 1);
+                        const double nan = __longlong_as_double(0x7FF8000000000000LL);
+                        double v0 = bad ? nan : ldexp(x96_to_double(w0[j], w1[j], w2[j]), E);
+                        if (CX) {
+                            double v1 = bad ? nan : ldexp(x96_to_double(w0[j + 1], w1[j + 1], w2[j + 1]), E);
+                            ((double2 *)Cl)[off] = make_double2(v0, v1);
+                        } else {
+                            ((double *)Cl)[off] = v0;
+                        }
+                    } else {
+                        if (CX) ((float2 *)Cl)[off] = make_float2(accf[j], accf[j + 1]);
+                        else ((float *)Cl)[off] = accf[j];
+                    }
                 }
             }
         }
@@ -806,6 +880,20 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                      "r"((uint32_t)TCOLS)
                      : "memory");
+}
+
+// A single contraction: its job in the parameter space (the tensor maps
+// must lie in param, const or global memory for TMA).
+template <int S, bool EXACT, bool CX>
+__global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(const __grid_constant__ OzJob job) {
+    oz_gemm_body<S, EXACT, CX>(OzOneJob{&job});
+}
+
+// A group: every bucket of one kernel variant in one persistent launch.
+template <int S, bool EXACT, bool CX>
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    k_oz_gemm_grouped(const OzJob *__restrict__ jobs, const int64_t *__restrict__ start, int njobs) {
+    oz_gemm_body<S, EXACT, CX>(OzJobTable{jobs, start, njobs});
 }
 
 // =============================================================================
@@ -900,42 +988,81 @@ static int make_map(CUtensorMap *tm, void *base, int64_t k_e, int64_t rows, int6
     return MGB_OK;
 }
 
+static int sm_count() {
+    static int count[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!count[dev & 63]) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        count[dev & 63] = n > 0 ? n : 1;
+    }
+    return count[dev & 63];
+}
+
+template <typename K>
+static int set_smem_attr(K kern, int smem, bool (&done)[64]) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!done[dev & 63]) {
+        MGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        done[dev & 63] = true;
+    }
+    return MGB_OK;
+}
+
+// Persistent grids: one CTA per SM (the shared memory of a CTA exceeds half
+// of an SM's), each walking its share of the tiles.
 template <int S, bool EXACT, bool CX>
-static int launch_gemm_t(const CUtensorMap &ta, const CUtensorMap &tb, const OzGemmArgs &a, dim3 grid,
-                         cudaStream_t s) {
+static int launch_gemm_t(const OzJob &job, int64_t tiles, cudaStream_t s) {
     auto kern = k_oz_gemm<S, EXACT, CX>;
     constexpr int smem = oz_smem_bytes(S);
     static bool attr_set[64] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (!attr_set[dev & 63]) {
-        MGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr_set[dev & 63] = true;
-    }
-    kern<<<grid, OZ_THREADS, smem, s>>>(ta, tb, a);
+    if (int st = set_smem_attr(kern, smem, attr_set)) return st;
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count());
+    kern<<<grid, OZ_THREADS, smem, s>>>(job);
     MGB_CUDA_CHECK(cudaGetLastError());
     return MGB_OK;
 }
 
-static int launch_gemm(int S, bool exact, bool cx, const CUtensorMap &ta, const CUtensorMap &tb,
-                       const OzGemmArgs &a, dim3 grid, cudaStream_t s) {
-    if (!exact) return cx ? launch_gemm_t<3, false, true>(ta, tb, a, grid, s)
-                          : launch_gemm_t<3, false, false>(ta, tb, a, grid, s);
-#define OZ_CASE(SS)                                                                  \
-    case SS:                                                                         \
-        return cx ? launch_gemm_t<SS, true, true>(ta, tb, a, grid, s)                \
-                  : launch_gemm_t<SS, true, false>(ta, tb, a, grid, s);
-    switch (S) {
-        OZ_CASE(3)
-        OZ_CASE(4)
-        OZ_CASE(5)
-        OZ_CASE(6)
-        OZ_CASE(7)
-        OZ_CASE(8)
-    }
-#undef OZ_CASE
-    return fail(MGB_ERR_ARGUMENT, "unsupported slice count");
+template <int S, bool EXACT, bool CX>
+static int launch_grouped_t(const OzJob *jobs, const int64_t *start, int njobs, int64_t tiles, cudaStream_t s) {
+    auto kern = k_oz_gemm_grouped<S, EXACT, CX>;
+    constexpr int smem = oz_smem_bytes(S);
+    static bool attr_set[64] = {};
+    if (int st = set_smem_attr(kern, smem, attr_set)) return st;
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count());
+    kern<<<grid, OZ_THREADS, smem, s>>>(jobs, start, njobs);
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
 }
+
+// Dispatch on (slices, exact, complex): BF16X3 is S = 3 and not exact.
+#define OZ_DISPATCH(CALL)                                                        \
+    if (!exact) return cx ? CALL(3, false, true) : CALL(3, false, false);       \
+    switch (S) {                                                                 \
+    case 3: return cx ? CALL(3, true, true) : CALL(3, true, false);             \
+    case 4: return cx ? CALL(4, true, true) : CALL(4, true, false);             \
+    case 5: return cx ? CALL(5, true, true) : CALL(5, true, false);             \
+    case 6: return cx ? CALL(6, true, true) : CALL(6, true, false);             \
+    case 7: return cx ? CALL(7, true, true) : CALL(7, true, false);             \
+    case 8: return cx ? CALL(8, true, true) : CALL(8, true, false);             \
+    }                                                                            \
+    return fail(MGB_ERR_ARGUMENT, "unsupported slice count");
+
+static int launch_gemm(int S, bool exact, bool cx, const OzJob &job, int64_t tiles, cudaStream_t s) {
+#define OZ_ONE(SS, EX, CC) launch_gemm_t<SS, EX, CC>(job, tiles, s)
+    OZ_DISPATCH(OZ_ONE)
+#undef OZ_ONE
+}
+
+static int launch_grouped(int S, bool exact, bool cx, const OzJob *jobs, const int64_t *start, int njobs,
+                          int64_t tiles, cudaStream_t s) {
+#define OZ_GRP(SS, EX, CC) launch_grouped_t<SS, EX, CC>(jobs, start, njobs, tiles, s)
+    OZ_DISPATCH(OZ_GRP)
+#undef OZ_GRP
+}
+#undef OZ_DISPATCH
 
 static int unit_row_fast(const ModeGroup &gr, const ModeGroup &gk, int t) {
     int64_t sr = gr.n > 0 ? std::llabs(gr.str[t][0]) : INT64_MAX;
@@ -970,8 +1097,9 @@ static int run_scale(const OpGeom &g, const void *X, int32_t *exps, int64_t L, c
     return MGB_OK;
 }
 
-int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C, void *ws,
-                 cudaStream_t s, cudaEvent_t mid) {
+// Pre-pass of the emulated forms: exponents (OZAKI) and slices of A and B
+// into the workspace.
+int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *ws, cudaStream_t s) {
     if (((uintptr_t)ws & 255) != 0) return fail(MGB_ERR_WORKSPACE, "workspace must be 256-byte aligned");
     const bool exact = p.form == MGB_FORM_OZAKI;
     const bool cx = is_complex(p.compute_dtype);
@@ -980,8 +1108,6 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
     uint32_t *sa = (uint32_t *)(w + p.ws_a), *sb = (uint32_t *)(w + p.ws_b);
     int32_t *ea = exact ? (int32_t *)(w + p.ws_scale_a) : nullptr;
     int32_t *eb = exact ? (int32_t *)(w + p.ws_scale_b) : nullptr;
-    int32_t *status = device_status_ptr();
-    if (!status) return fail(MGB_ERR_CUDA, "device status word unavailable");
 
     OpGeom ga, gb;
     ga.ptrs = p.pa;
@@ -1014,20 +1140,31 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
                                   : run_prepass<float, true>(gb, mode_b, B, nullptr, 3, sb, p.n_e, kw, p.L, s);
         if (st) return st;
     }
-    if (mid) MGB_CUDA_CHECK(cudaEventRecord(mid, s));
-    CUtensorMap ta, tb;
-    if ((st = make_map(&ta, sa, p.k_e, p.m_e, p.L * S, p.kpad, OZ_BM, S))) return st;
+    return MGB_OK;
+}
+
+// The GEMM's view of a plan whose slices lie in `ws`.
+static int ozaki_job(const ContractionPlan &p, void *C, void *ws, OzJob &job, int64_t &tiles) {
+    const bool exact = p.form == MGB_FORM_OZAKI;
+    const int S = p.slices;
+    uint8_t *w = (uint8_t *)ws;
+    uint32_t *sa = (uint32_t *)(w + p.ws_a), *sb = (uint32_t *)(w + p.ws_b);
+    int32_t *status = device_status_ptr();
+    if (!status) return fail(MGB_ERR_CUDA, "device status word unavailable");
+    std::memset(&job, 0, sizeof(job));
+    int st;
+    if ((st = make_map(&job.tmA, sa, p.k_e, p.m_e, p.L * S, p.kpad, OZ_BM, S))) return st;
     const int bn = oz_bn(S);
-    if ((st = make_map(&tb, sb, p.k_e, p.n_e, p.L * S, p.kpad, bn, S))) return st;
-    OzGemmArgs a;
+    if ((st = make_map(&job.tmB, sb, p.k_e, p.n_e, p.L * S, p.kpad, bn, S))) return st;
+    OzGemmArgs &a = job.a;
     a.M = p.M;
     a.Ne = p.n_e;
     a.N = p.N;
     a.nkb = (int32_t)((p.k_e + OZ_BK - 1) / OZ_BK);
     a.kcb = exact ? oz_chunk_blocks(S) : OZ_KC / OZ_BK;
     a.S = S;
-    a.expA = ea;
-    a.expB = eb;
+    a.expA = exact ? (int32_t *)(w + p.ws_scale_a) : nullptr;
+    a.expB = exact ? (int32_t *)(w + p.ws_scale_b) : nullptr;
     a.C = C;
     a.cptr = p.pc;
     a.band = p.band > 0 ? p.band : OZ_GROUP_M;
@@ -1037,10 +1174,84 @@ int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C
     a.status = status;
     if (a.gm.n == 0) { a.gm.n = 1; a.gm.ext[0] = 1; for (int t = 0; t < 3; ++t) a.gm.str[t][0] = 0; }
     if (a.gn.n == 0) { a.gn.n = 1; a.gn.ext[0] = 1; for (int t = 0; t < 3; ++t) a.gn.str[t][0] = 0; }
-    dim3 grid((unsigned)((p.n_e + bn - 1) / bn), (unsigned)((p.M + OZ_BM - 1) / OZ_BM),
-              (unsigned)p.L);
-    if ((p.M + OZ_BM - 1) / OZ_BM > 65535) return fail(MGB_ERR_UNSUPPORTED, "M too large for the grid");
-    return launch_gemm(S, exact, cx, ta, tb, a, grid, s);
+    job.tiles_n = (int32_t)((p.n_e + bn - 1) / bn);
+    job.tiles_m = (int32_t)((p.M + OZ_BM - 1) / OZ_BM);
+    job.L = (int32_t)p.L;
+    if ((p.n_e + bn - 1) / bn > INT32_MAX || (p.M + OZ_BM - 1) / OZ_BM > INT32_MAX || p.L > INT32_MAX)
+        return fail(MGB_ERR_UNSUPPORTED, "contraction too large for the tile grid");
+    tiles = (int64_t)job.tiles_n * job.tiles_m * job.L;
+    return MGB_OK;
+}
+
+int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C, void *ws,
+                 cudaStream_t s, cudaEvent_t mid) {
+    int st = ozaki_prepass(p, A, B, ws, s);
+    if (st) return st;
+    if (mid) MGB_CUDA_CHECK(cudaEventRecord(mid, s));
+    OzJob job;
+    int64_t tiles = 0;
+    if ((st = ozaki_job(p, C, ws, job, tiles))) return st;
+    return launch_gemm(p.slices, p.form == MGB_FORM_OZAKI, is_complex(p.compute_dtype), job, tiles, s);
+}
+
+// ---- one persistent GEMM launch for several plans of one kernel variant ----
+struct OzGrouped {
+    int S = 0;
+    bool exact = false, cx = false;
+    int njobs = 0;
+    int64_t tiles = 0;
+    OzJob *jobs = nullptr;     // device
+    int64_t *start = nullptr;  // device [njobs + 1]
+};
+
+int ozaki_grouped_create(const std::vector<const ContractionPlan *> &plans, const std::vector<void *> &ws,
+                         OzGrouped **out) {
+    *out = nullptr;
+    if (plans.empty()) return fail(MGB_ERR_ARGUMENT, "grouped GEMM: no plans");
+    auto *g = new OzGrouped();
+    g->S = plans[0]->slices;
+    g->exact = plans[0]->form == MGB_FORM_OZAKI;
+    g->cx = is_complex(plans[0]->compute_dtype);
+    std::vector<OzJob> host(plans.size());
+    std::vector<int64_t> start(plans.size() + 1, 0);
+    for (size_t i = 0; i < plans.size(); ++i) {
+        const ContractionPlan &p = *plans[i];
+        if (p.slices != g->S || (p.form == MGB_FORM_OZAKI) != g->exact || is_complex(p.compute_dtype) != g->cx) {
+            delete g;
+            return fail(MGB_ERR_ARGUMENT, "grouped GEMM: plans of different kernel variants");
+        }
+        int64_t t = 0;
+        if (int st = ozaki_job(p, nullptr, ws[i], host[i], t)) {
+            delete g;
+            return st;
+        }
+        start[i + 1] = start[i] + t;
+    }
+    g->njobs = (int)plans.size();
+    g->tiles = start.back();
+    cudaError_t e = cudaMalloc((void **)&g->jobs, host.size() * sizeof(OzJob));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&g->start, start.size() * sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaMemcpy(g->jobs, host.data(), host.size() * sizeof(OzJob), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(g->start, start.data(), start.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        ozaki_grouped_destroy(g);
+        return cuda_fail(e, "grouped GEMM job table");
+    }
+    *out = g;
+    return MGB_OK;
+}
+
+int ozaki_grouped_launch(const OzGrouped *g, cudaStream_t s) {
+    if (g->tiles == 0) return MGB_OK;
+    return launch_grouped(g->S, g->exact, g->cx, g->jobs, g->start, g->njobs, g->tiles, s);
+}
+
+void ozaki_grouped_destroy(OzGrouped *g) {
+    if (!g) return;
+    if (g->jobs) cudaFree(g->jobs);
+    if (g->start) cudaFree(g->start);
+    delete g;
 }
 
 }  // namespace mgb

@@ -96,6 +96,8 @@ SIGNATURES = {
     "mgb_group_execute": (_i32, [_vp, _vp, _u64, _vp]),
     "mgb_group_set_tiles": (_i32, [_vp, _P(_i32)]),
     "mgb_group_execute_part": (_i32, [_vp, _i32, _i32, _vp, _u64, _vp]),
+    "mgb_group_prepare_part": (_i32, [_vp, _i32, _i32, _vp, _u64, _vp]),
+    "mgb_group_finish": (_i32, [_vp, _vp, _u64, _vp]),
     "mgb_group_destroy": (_i32, [_vp]),
     "mgb_server_create": (_i32, [_P(_vp), _u64, _i32, _i32]),
     "mgb_server_submit": (_i32, [_vp, _vp, _vp, _vp, _vp, _u64, _vp, _P(ctypes.c_int64)]),

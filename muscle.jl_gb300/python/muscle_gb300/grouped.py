@@ -83,25 +83,35 @@ class Group:
         lib = _lib.load()
         check(lib.mgb_group_update(self.handle, *self._pointer_arrays()), lib)
 
-    def execute(self, stream: torch.cuda.Stream | None = None, parts: int = 1):
-        """Runs every member on `stream` (default: the current stream). With
-        parts > 1 the members are split into that many parts of about equal
-        work, run on side streams forked from and joined back into `stream`
-        (the parts write disjoint outputs and workspace slices)."""
+    def execute(self, stream: torch.cuda.Stream | None = None, parts: int = 1, persistent: bool = True):
+        """Runs every member on `stream` (default: the current stream).
+
+        persistent: the emulated buckets' tensor-core work runs as one
+        persistent launch per kernel variant (after all pre-passes);
+        otherwise every bucket runs its own launches. With parts > 1 the
+        pre-passes (persistent) or whole buckets (not persistent) are split
+        into that many parts of about equal work, run on side streams forked
+        from and joined back into `stream` (the parts write disjoint outputs
+        and workspace slices)."""
         lib = _lib.load()
         main = stream if stream is not None else torch.cuda.current_stream(self.device)
+        ws, wsb = self.workspace.data_ptr(), self.workspace_bytes
         if parts <= 1:
-            check(lib.mgb_group_execute(self.handle, self.workspace.data_ptr(), self.workspace_bytes,
-                                        main.cuda_stream), lib)
+            if persistent:
+                check(lib.mgb_group_execute(self.handle, ws, wsb, main.cuda_stream), lib)
+            else:
+                check(lib.mgb_group_execute_part(self.handle, 0, 1, ws, wsb, main.cuda_stream), lib)
             return
         side = self._side_streams(parts)
         for ss in side:
             ss.wait_stream(main)
+        fn = lib.mgb_group_prepare_part if persistent else lib.mgb_group_execute_part
         for i, ss in enumerate(side):
-            check(lib.mgb_group_execute_part(self.handle, i, parts, self.workspace.data_ptr(), self.workspace_bytes,
-                                             ss.cuda_stream), lib)
+            check(fn(self.handle, i, parts, ws, wsb, ss.cuda_stream), lib)
         for ss in side:
             main.wait_stream(ss)
+        if persistent:
+            check(lib.mgb_group_finish(self.handle, ws, wsb, main.cuda_stream), lib)
 
     def _side_streams(self, parts):
         cache = getattr(self, "_side", None)
@@ -110,18 +120,19 @@ class Group:
             self._side = cache
         return cache
 
-    def capture(self, parts: int = 1) -> torch.cuda.CUDAGraph:
-        """Warm up once, then record execute() into a CUDA graph (with parts > 1
-        the parts become parallel branches of the graph)."""
+    def capture(self, parts: int = 1, persistent: bool = True) -> torch.cuda.CUDAGraph:
+        """Warm up once (which also uploads the persistent launches' job
+        tables), then record execute() into a CUDA graph (with parts > 1 the
+        parts become parallel branches of the graph)."""
         s = torch.cuda.Stream(self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):
-            self.execute(s, parts)
+            self.execute(s, parts, persistent)
         torch.cuda.current_stream(self.device).wait_stream(s)
         torch.cuda.synchronize(self.device)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            self.execute(torch.cuda.current_stream(self.device), parts)
+            self.execute(torch.cuda.current_stream(self.device), parts, persistent)
         return g
 
     def __del__(self):

@@ -94,7 +94,9 @@ def test_group_graph_capture_and_update():
 
 def test_group_parts_and_parallel_graph_branches():
     """The members split into parts on side streams (parallel branches of one
-    captured graph) give results bit-identical to the one-stream execution."""
+    captured graph), with the tensor-core work in one persistent launch per
+    kernel variant or in every bucket's own launches, give results
+    bit-identical to the one-stream execution."""
     import muscle_gb300 as m
 
     insts = instances(60, 1300, np.complex128)
@@ -103,18 +105,20 @@ def test_group_parts_and_parallel_graph_branches():
     g.execute()
     torch.cuda.synchronize()
     ref_out = [C.data.clone() for C, _, _ in items]
-    for parts in (2, 3, 7):
+    for parts in (1, 2, 3, 7):
+        for persistent in (True, False):
+            for C, _, _ in items:
+                C.data.zero_()
+            g.execute(parts=parts, persistent=persistent)
+            torch.cuda.synchronize()
+            assert all(torch.equal(C.data, r) for (C, _, _), r in zip(items, ref_out)), (parts, persistent)
+    for persistent in (True, False):
+        graph = g.capture(parts=4, persistent=persistent)
         for C, _, _ in items:
             C.data.zero_()
-        g.execute(parts=parts)
+        graph.replay()
         torch.cuda.synchronize()
-        assert all(torch.equal(C.data, r) for (C, _, _), r in zip(items, ref_out)), parts
-    graph = g.capture(parts=4)
-    for C, _, _ in items:
-        C.data.zero_()
-    graph.replay()
-    torch.cuda.synchronize()
-    assert all(torch.equal(C.data, r) for (C, _, _), r in zip(items, ref_out))
+        assert all(torch.equal(C.data, r) for (C, _, _), r in zip(items, ref_out)), persistent
     assert m.device_status() == 0
 
 
