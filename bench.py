@@ -311,6 +311,41 @@ def serve_bench(dev, rates, seconds, n_requests=192, seed=5, budget=120 * 10**9,
     return res
 
 
+def _group_phases_ms(dev, g, steps):
+    """Device time of a group's two phases, each replayed as its own graph:
+    the pre-passes (and plain buckets), then the persistent tensor-core
+    launches."""
+    import torch
+
+    from muscle_gb300 import _lib
+
+    lib = _lib.load()
+    wsp, wsb = g.workspace.data_ptr(), g.workspace_bytes
+    out = {}
+    for name, fn in (("prepass_and_plain", lambda st: lib.mgb_group_prepare_part(g.handle, 0, 1, wsp, wsb, st)),
+                     ("persistent_gemm", lambda st: lib.mgb_group_finish(g.handle, wsp, wsb, st))):
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            _lib.check(fn(side.cuda_stream), lib)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            _lib.check(fn(torch.cuda.current_stream(dev).cuda_stream), lib)
+        graph.replay()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            graph.replay()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        out[name] = e0.elapsed_time(e1) / steps
+        del graph
+    return out
+
+
 def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
     """Batching form: PEPS-style pairs, one group per element type, autotuned
     schedule, replayed as one CUDA graph."""
@@ -347,7 +382,7 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
         by_parts = {}
         # (branches, persistent): one persistent tensor-core launch per kernel
         # variant after the pre-passes, or every bucket's own launches
-        for parts, pers in ((1, True), (4, True), (4, False)):
+        for parts, pers in ((1, True), (4, True), (4, False), (8, False)):
             graph = g.capture(parts, pers)
             for _ in range(3):
                 graph.replay()
@@ -362,6 +397,27 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
             del graph
         best_parts = min(by_parts, key=by_parts.get)
         ms = by_parts[best_parts]
+        # the persistent form's two phases on their own: pre-passes (and plain
+        # buckets), then the persistent tensor-core launches
+        phase_ms = _group_phases_ms(dev, g, steps)
+        by_class = []
+        if tdt == torch.complex128:
+            # every (M, N, K) class as a group of its own: where the time goes
+            classes = {}
+            for it, (sa, ia, sb, ib, ic) in zip(items, shapes):
+                ext = dict(zip(ia + ib, sa + sb))
+                mnk = tuple(int(np.prod([ext[x] for x in lab if x in ext])) for lab in
+                            ([x for x in ia if x not in ib], [x for x in ib if x not in ia],
+                             [x for x in ia if x in ib and x not in ic]))
+                classes.setdefault(mnk, []).append(it)
+            for (M, N, K), its in sorted(classes.items(), key=lambda kv: -kv[0][0] * kv[0][1] * kv[0][2] * len(kv[1])):
+                gc = m.Group(its, "ozaki")
+                ph = _group_phases_ms(dev, gc, 3)
+                kb = -(-M // 128) * -(-2 * N // 32) * -(-2 * K // 32) * len(its)
+                by_class.append({"M": M, "N": N, "K": K, "members": len(its), "k_blocks": kb, **ph,
+                                 "k_blocks_per_ms": kb / ph["persistent_gemm"]})
+                del gc
+                torch.cuda.empty_cache()
         # one at a time, plain form, on the first 256 instances
         sub = items[:256]
         torch.cuda.synchronize(dev)
@@ -377,6 +433,7 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
         key = "c64" if tdt == torch.complex128 else "c32"
         out[key] = {"graph_ms": ms, "graph_branches": best_parts[0], "persistent": best_parts[1],
                     "graph_ms_by_branches": {f"{k[0]}{'p' if k[1] else ''}": v for k, v in by_parts.items()},
+                    "persistent_phases_ms": phase_ms, "by_class": by_class,
                     "tflops": flops / (ms / 1e3) / 1e12, "contractions_per_s": len(items) / (ms / 1e3),
                     "one_at_a_time_plain_per_s": one, "forms_chosen": forms, "gflop": flops / 1e9,
                     "distinct_plans": len({id(p) for p in g.plans})}

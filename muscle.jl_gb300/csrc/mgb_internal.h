@@ -55,15 +55,20 @@ struct ModeGroup {
     }
 };
 
-// Device-side decomposition: offset of linear index `idx` in tensor `t`.
+// Device-side decomposition: offset of linear index `idx` (0 <= idx < size())
+// in tensor `t`. The slowest mode needs no division, and indices below 2^31
+// divide in 32 bits (a 64-bit division is a long software sequence on the GPU).
 __host__ __device__ inline int64_t group_offset(const ModeGroup &g, int t, int64_t idx) {
     int64_t off = 0;
-    for (int i = 0; i < g.n; ++i) {
-        int64_t e = g.ext[i];
-        int64_t q = idx / e;
+    for (int i = 0; i + 1 < g.n; ++i) {
+        const int64_t e = g.ext[i];
+        int64_t q;
+        if ((uint64_t)idx <= 0x7FFFFFFFu && (uint64_t)e <= 0x7FFFFFFFu) q = (int64_t)((uint32_t)idx / (uint32_t)e);
+        else q = idx / e;
         off += (idx - q * e) * g.str[t][i];
         idx = q;
     }
+    if (g.n > 0) off += idx * g.str[t][g.n - 1];
     return off;
 }
 

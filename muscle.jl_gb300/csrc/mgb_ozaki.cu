@@ -14,9 +14,10 @@
 //   W = 8) the epilogue warps read every group's float32 partial sums (exact
 //   integers), convert them to int and add them, shifted left by
 //   W (S + 1 - d), into one exact 96-bit integer per output element
-//   (|X| < 2^(log2 K + W (S + 1) + 1) < 2^95 for any K below 2^31). The only
-//   float64 arithmetic left is the conversion of X and one ldexp per output
-//   element (GB300's FP64 pipe is slow).
+//   (|X| < 2^(log2 K + W (S + 1) + 1) < 2^95 for any K below 2^31). X times
+//   the row and column scales is rounded to float64 with integer operations
+//   only (x96_ldexp_rn): no float64 arithmetic at all, since GB300's FP64
+//   pipe retires about two operations per cycle per SM.
 //   Group bound per k: max(d + 1, 4) * 2^(2W-2); KC * bound <= 2^24 for
 //   d <= 15 (W = 7) and d <= 7 (W = 8), which covers every group of every
 //   supported S (d <= S + 1).
@@ -33,7 +34,7 @@
 // B_e[2n+q][2k+p] holds [[Br, -Bi], [Bi, Br]] so that C_e[m][2n+q] is part q
 // of C[m,n] (4 real products per complex product, as zgemm's 4M form).
 //
-// Pipeline per CTA (128 x BN embedded outputs, BN = 32, or 64 for S = 3;
+// Pipeline per CTA (128 x BN embedded outputs, BN = 32, or 64 for BF16X3;
 // one CTA per SM):
 //   warp 0       TMA producer: one 3-D box per operand per 32-wide k block
 //                loads all S slices at once into a 64B-swizzled stage;
@@ -60,6 +61,7 @@
 #include <vector>
 
 #include "mgb_internal.h"
+#include "mgb_x96.h"
 
 namespace mgb {
 
@@ -83,9 +85,11 @@ constexpr long long OZ_TIMEOUT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 // Columns per digit group (= embedded rows of B per CTA): two banks of S
 // groups must fit the 512 TMEM columns, and one MMA covers at most 256.
-__host__ __device__ constexpr int oz_bn(int S) { return S <= 3 ? 64 : 32; }
-__host__ __device__ constexpr int oz_b_tile(int S) { return oz_bn(S) * OZ_BK * 2; }  // bytes per slice
-__host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (OZ_A_TILE + oz_b_tile(S)); }
+// BF16X3 (S = 3, two float registers per column) takes 64; the exact forms
+// keep 32, where their three 32-bit words per column stay in registers.
+__host__ __device__ constexpr int oz_bn(int S, bool exact) { return (!exact && S <= 3) ? 64 : 32; }
+__host__ __device__ constexpr int oz_b_tile(int S, bool exact) { return oz_bn(S, exact) * OZ_BK * 2; }  // bytes per slice
+__host__ __device__ constexpr int oz_stage_bytes(int S, bool exact) { return S * (OZ_A_TILE + oz_b_tile(S, exact)); }
 // Digit width and exact chunk length (in 32-wide k blocks) per slice count.
 // W = 8 for S <= 6: |s1| <= 256, |si| <= 128, group bound max(d+1,4) 2^14, so a
 // float32 accumulator stays exact over 4 blocks (128 k) for every d <= 7.
@@ -93,17 +97,20 @@ __host__ __device__ constexpr int oz_stage_bytes(int S) { return S * (OZ_A_TILE 
 // for d <= 15. Both hold about the same number of mantissa bits (W S = 48 / 49).
 __host__ __device__ constexpr int oz_digit_bits(int S) { return S <= 6 ? 8 : 7; }
 __host__ __device__ constexpr int oz_chunk_blocks(int S) { return oz_digit_bits(S) == 8 ? 4 : 8; }
-__host__ __device__ constexpr int oz_stages(int S) {
-    return (OZ_SMEM_BUDGET / oz_stage_bytes(S)) < OZ_MAX_STAGES ? (OZ_SMEM_BUDGET / oz_stage_bytes(S))
-                                                                : OZ_MAX_STAGES;
+__host__ __device__ constexpr int oz_stages(int S, bool exact) {
+    return (OZ_SMEM_BUDGET / oz_stage_bytes(S, exact)) < OZ_MAX_STAGES ? (OZ_SMEM_BUDGET / oz_stage_bytes(S, exact))
+                                                                       : OZ_MAX_STAGES;
 }
-// two banks of S groups of oz_bn(S) columns; bank bases at columns 0 and 256
+// two banks of S groups of oz_bn columns; bank bases at columns 0 and 256
 __host__ __device__ constexpr int oz_tmem_cols(int) { return 512; }
 // More than half of the SM's shared memory for every S, so one CTA (and one
 // TMEM allocation) per SM.
-__host__ __device__ constexpr int oz_smem_bytes(int S) {
-    return oz_stages(S) * oz_stage_bytes(S) + 1024 /*align*/ + 256 /*barriers*/;
+__host__ __device__ constexpr int oz_smem_bytes(int S, bool exact) {
+    return oz_stages(S, exact) * oz_stage_bytes(S, exact) + 1024 /*align*/ + 256 /*barriers*/;
 }
+static_assert(2 * oz_smem_bytes(3, true) > 228 * 1024 && 2 * oz_smem_bytes(8, true) > 228 * 1024 &&
+                  2 * oz_smem_bytes(3, false) > 228 * 1024,
+              "one CTA per SM");
 
 // =============================================================================
 // PTX wrappers
@@ -220,10 +227,6 @@ __device__ __forceinline__ void add96(uint32_t &w0, uint32_t &w1, uint32_t &w2, 
 }
 __device__ __forceinline__ void add64hi(uint32_t &w1, uint32_t &w2, uint32_t a1, uint32_t a2) {
     asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(w1), "+r"(w2) : "r"(a1), "r"(a2));
-}
-__device__ __forceinline__ double x96_to_double(uint32_t w0, uint32_t w1, uint32_t w2) {
-    int64_t hi = (int64_t)(((uint64_t)w2 << 32) | w1);  // X = hi * 2^32 + w0
-    return fma(__ll2double_rn(hi), 4294967296.0, __uint2double_rn(w0));
 }
 
 // K-major operand tile, 64-byte swizzle: rows of 64 B, 8-row atoms of 512 B.
@@ -565,15 +568,16 @@ __device__ __forceinline__ void oz_tile(const OzJob &J, int64_t local, int bn, i
 // of A slice i with B slices 0 .. S-1-i are ONE tcgen05.mma with
 // N = BN (S - i) whose accumulator columns are exactly groups i .. S-1:
 // S wide MMAs per 16 k instead of S (S+1)/2 narrow ones, and every A slice
-// is read from shared memory once per 16 k. BN = 64 for S = 3 (BF16X3
-// included) and 32 for S >= 4: the widest that two banks leave room for
-// while the epilogue's 96-bit accumulators stay in registers.
+// is read from shared memory once per 16 k. BN = 64 for BF16X3 and 32 for
+// the exact forms: the widest that two banks leave room for while the
+// epilogue's accumulators (96-bit integers, or float sums and their
+// compensations) stay in registers.
 template <int S, bool EXACT, bool CX, typename Src>
 __device__ __forceinline__ void oz_gemm_body(const Src &src) {
     constexpr int W = oz_digit_bits(S);  // digit width (EXACT)
-    constexpr int NST = oz_stages(S);
-    constexpr int STAGE = oz_stage_bytes(S);
-    constexpr int BN = oz_bn(S);     // columns per digit group, embedded B rows per CTA
+    constexpr int NST = oz_stages(S, EXACT);
+    constexpr int STAGE = oz_stage_bytes(S, EXACT);
+    constexpr int BN = oz_bn(S, EXACT);  // columns per digit group, embedded B rows per CTA
     constexpr int HALF = BN / 2;     // columns per group read by one epilogue warp
     constexpr int TCOLS = oz_tmem_cols(S);
     constexpr int BANK = TCOLS / 2;  // TMEM column offset of the second bank
@@ -756,6 +760,34 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
             oz_tile(J, local, BN, m0, n0, l);
             const int64_t row = m0 + 32 * q + lane;
             const int nchunks = (args.nkb + args.kcb - 1) / args.kcb;
+            // Output addressing of the tile, fetched before the first chunk
+            // wait so that its loads overlap the MMAs: the thread's row (offset
+            // and exponent), and one output column per lane (lane j < NCOL
+            // holds column j of this warp's half, broadcast by shuffles).
+            constexpr int NCOL = CX ? HALF / 2 : HALF;
+            const bool row_ok = row < args.M;
+            int64_t rowoff = 0;
+            int erow = 0;
+            bool badrow = false;
+            if (row_ok) {
+                rowoff = (args.cptr ? 0 : group_offset(args.gl, 2, l)) + group_offset(args.gm, 2, row);
+                if (EXACT) {
+                    const int be = args.expA[(int64_t)l * args.M + row];
+                    badrow = be == 0x7FF;
+                    erow = be == 0 ? -1022 : be - 1022;
+                }
+            }
+            long long lcoff = 0;
+            int lexp = -1;  // the column's exponent (0 without one), -1 beyond the output
+            {
+                const int64_t ne = n0 + HALF * h + (int64_t)lane * (CX ? 2 : 1);
+                if (lane < NCOL && ne < args.Ne) {
+                    const int64_t n = CX ? (ne >> 1) : ne;
+                    lcoff = group_offset(args.gn, 2, n);
+                    lexp = EXACT ? args.expB[(int64_t)l * args.N + n] : 0;
+                }
+            }
+            void *const Cl = args.cptr ? args.cptr[l] : args.C;
             // EXACT: one 96-bit two's-complement integer per output column,
             // X = sum_d G_d 2^(W (S + 1 - d)), held in w0 (bits 0-31), w1, w2.
             uint32_t w0[EXACT ? HALF : 1], w1[EXACT ? HALF : 1], w2[EXACT ? HALF : 1];
@@ -775,7 +807,8 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
 #pragma unroll 1
             for (int c = 0; c < nchunks; ++c, ++C) {
                 const uint32_t bank = C & 1u;
-                if (!mbar_wait(smem_u32(acc_full + bank), (C >> 1) & 1u, abort_flag, status)) {
+                // warp-uniform outcome: the warp-collective loads below need every lane
+                if (!__all_sync(0xffffffffu, mbar_wait(smem_u32(acc_full + bank), (C >> 1) & 1u, abort_flag, status))) {
                     ok = false;
                     break;
                 }
@@ -811,11 +844,24 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
                         }
                     }
                 } else {
-                    // pieces hi*hi, then the products of piece-index sum 1 and 2
-                    uint32_t v0[HALF], v1[HALF], v2[HALF];
-                    tc_ld<HALF>(tb, v0);
-                    tc_ld<HALF>(tb + BN, v1);
-                    tc_ld<HALF>(tb + 2 * BN, v2);
+                    // pieces hi*hi, then the products of piece-index sum 1 and 2;
+                    // 16 columns at a time, so that the three groups' registers
+                    // stay beside the running sums and their compensations
+#pragma unroll
+                    for (int c2 = 0; c2 < HALF; c2 += 16) {
+                        uint32_t v0[16], v1[16], v2[16];
+                        tc_ld<16>(tb + c2, v0);
+                        tc_ld<16>(tb + BN + c2, v1);
+                        tc_ld<16>(tb + 2 * BN + c2, v2);
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            float x = __uint_as_float(v0[j]) + (__uint_as_float(v1[j]) + __uint_as_float(v2[j]));
+                            float y = x - comp[c2 + j];
+                            float s2 = accf[c2 + j] + y;
+                            comp[c2 + j] = (s2 - accf[c2 + j]) - y;
+                            accf[c2 + j] = s2;
+                        }
+                    }
 #pragma unroll
                     for (int g = 0; g < 3; ++g)
 #pragma unroll
@@ -824,51 +870,30 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(smem_u32(acc_empty + bank));
-#pragma unroll
-                    for (int j = 0; j < HALF; ++j) {
-                        float x = __uint_as_float(v0[j]) + (__uint_as_float(v1[j]) + __uint_as_float(v2[j]));
-                        float y = x - comp[j];
-                        float s2 = accf[j] + y;
-                        comp[j] = (s2 - accf[j]) - y;
-                        accf[j] = s2;
-                    }
                 }
             }
             if (!ok) break;
-            if (row < args.M) {
-                void *const Cl = args.cptr ? args.cptr[l] : args.C;
-                const int64_t lb = args.cptr ? 0 : group_offset(args.gl, 2, l);
-                const int64_t om = group_offset(args.gm, 2, row);
-                int erow = 0;
-                bool badrow = false;
-                if (EXACT) {
-                    int be = args.expA[(int64_t)l * args.M + row];
-                    badrow = be == 0x7FF;
-                    erow = be == 0 ? -1022 : be - 1022;
-                }
 #pragma unroll
-                for (int j = 0; j < HALF; j += (CX ? 2 : 1)) {
-                    int64_t ne = n0 + HALF * h + j;
-                    if (ne >= args.Ne) continue;
-                    int64_t n = CX ? (ne >> 1) : ne;
-                    int64_t off = lb + om + group_offset(args.gn, 2, n);
-                    if (EXACT) {
-                        int bc = args.expB[(int64_t)l * args.N + n];
-                        bool bad = badrow || bc == 0x7FF;
-                        int ecol = bc == 0 ? -1022 : bc - 1022;
-                        const int E = erow + ecol - W * (S + 1);
-                        const double nan = __longlong_as_double(0x7FF8000000000000LL);
-                        double v0 = bad ? nan : ldexp(x96_to_double(w0[j], w1[j], w2[j]), E);
-                        if (CX) {
-                            double v1 = bad ? nan : ldexp(x96_to_double(w0[j + 1], w1[j + 1], w2[j + 1]), E);
-                            ((double2 *)Cl)[off] = make_double2(v0, v1);
-                        } else {
-                            ((double *)Cl)[off] = v0;
-                        }
+            for (int jj = 0; jj < NCOL; ++jj) {
+                const int64_t coff = __shfl_sync(0xffffffffu, lcoff, jj);
+                const int bc = __shfl_sync(0xffffffffu, lexp, jj);
+                if (!row_ok || bc < 0) continue;
+                const int j = CX ? 2 * jj : jj;
+                const int64_t off = rowoff + coff;
+                if (EXACT) {
+                    const bool bad = badrow || bc == 0x7FF;
+                    const int E = erow + (bc == 0 ? -1022 : bc - 1022) - W * (S + 1);
+                    const double nan = __longlong_as_double(0x7FF8000000000000LL);
+                    const double v0 = bad ? nan : x96_ldexp_rn(w0[j], w1[j], w2[j], E);
+                    if (CX) {
+                        const double v1 = bad ? nan : x96_ldexp_rn(w0[j + 1], w1[j + 1], w2[j + 1], E);
+                        ((double2 *)Cl)[off] = make_double2(v0, v1);
                     } else {
-                        if (CX) ((float2 *)Cl)[off] = make_float2(accf[j], accf[j + 1]);
-                        else ((float *)Cl)[off] = accf[j];
+                        ((double *)Cl)[off] = v0;
                     }
+                } else {
+                    if (CX) ((float2 *)Cl)[off] = make_float2(accf[j], accf[j + 1]);
+                    else ((float *)Cl)[off] = accf[j];
                 }
             }
         }
@@ -1016,7 +1041,7 @@ static int set_smem_attr(K kern, int smem, bool (&done)[64]) {
 template <int S, bool EXACT, bool CX>
 static int launch_gemm_t(const OzJob &job, int64_t tiles, cudaStream_t s) {
     auto kern = k_oz_gemm<S, EXACT, CX>;
-    constexpr int smem = oz_smem_bytes(S);
+    constexpr int smem = oz_smem_bytes(S, EXACT);
     static bool attr_set[64] = {};
     if (int st = set_smem_attr(kern, smem, attr_set)) return st;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count());
@@ -1028,7 +1053,7 @@ static int launch_gemm_t(const OzJob &job, int64_t tiles, cudaStream_t s) {
 template <int S, bool EXACT, bool CX>
 static int launch_grouped_t(const OzJob *jobs, const int64_t *start, int njobs, int64_t tiles, cudaStream_t s) {
     auto kern = k_oz_gemm_grouped<S, EXACT, CX>;
-    constexpr int smem = oz_smem_bytes(S);
+    constexpr int smem = oz_smem_bytes(S, EXACT);
     static bool attr_set[64] = {};
     if (int st = set_smem_attr(kern, smem, attr_set)) return st;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count());
@@ -1154,7 +1179,7 @@ static int ozaki_job(const ContractionPlan &p, void *C, void *ws, OzJob &job, in
     std::memset(&job, 0, sizeof(job));
     int st;
     if ((st = make_map(&job.tmA, sa, p.k_e, p.m_e, p.L * S, p.kpad, OZ_BM, S))) return st;
-    const int bn = oz_bn(S);
+    const int bn = oz_bn(S, exact);
     if ((st = make_map(&job.tmB, sb, p.k_e, p.n_e, p.L * S, p.kpad, bn, S))) return st;
     OzGemmArgs &a = job.a;
     a.M = p.M;

@@ -153,6 +153,23 @@ def test_ozaki_exact_on_integer_data():
     assert np.array_equal(gotc, wantc)
 
 
+@pytest.mark.parametrize("slices", range(3, 9))
+def test_ozaki_every_slice_count_exact_on_16_bit_integers(slices):
+    """Integers below 2^16 need two 8-bit (or three 7-bit) digits after the
+    row and column scaling, so every slice count from 3 up must reproduce the
+    exact product bit for bit, real and complex, including ragged tiles."""
+    rng = np.random.default_rng(40 + slices)
+    a = rng.integers(-(2**16) + 1, 2**16, size=(200, 1100)).astype(np.float64)
+    b = rng.integers(-(2**16) + 1, 2**16, size=(1100, 70)).astype(np.float64)
+    want = a @ b  # |sum| < 2^43
+    got, _ = run(np.asfortranarray(a), ["i", "j"], np.asfortranarray(b), ["j", "k"], ["i", "k"], "ozaki", slices)
+    assert np.array_equal(got, want), slices
+    ac = (a + 1j * a[::-1]).copy(order="F")
+    bc = (b - 1j * b[:, ::-1]).copy(order="F")
+    gotc, _ = run(ac, ["i", "j"], bc, ["j", "k"], ["i", "k"], "ozaki", slices)
+    assert np.array_equal(gotc, ac @ bc), slices
+
+
 def test_ozaki_slice_sweep_and_loguniform_spread():
     """Config-3 pattern (log-uniform magnitudes over 2^-20..2^20) at a reduced
     size: error falls with the slice count and S >= 7 meets 1e-13."""
