@@ -508,7 +508,7 @@ struct OzGemmArgs {
 // One contraction (or one bucket of a group) as the GEMM sees it: the slice
 // tensor maps, the arguments and its tile grid (column tiles x row tiles x
 // batch entries).
-struct alignas(64) OzJob {
+struct OzJob {  // aligned as its tensor maps
     CUtensorMap tmA, tmB;
     OzGemmArgs a;
     int32_t tiles_n, tiles_m, L;
@@ -516,10 +516,13 @@ struct alignas(64) OzJob {
 
 // Tile sources of the kernel: one job in the parameter space, or a table of
 // jobs in global memory (a group) whose tiles are numbered consecutively.
+// `hint` is the caller's job index of its previous tile (0 at first): a CTA
+// visits its tiles in increasing order, so the next tile usually lies in the
+// same job or the one after it.
 struct OzOneJob {
     const OzJob *j;
     __device__ int64_t tiles() const { return (int64_t)j->tiles_n * j->tiles_m * j->L; }
-    __device__ const OzJob &job(int64_t t, int64_t &local) const {
+    __device__ const OzJob &job(int64_t t, int64_t &local, int &) const {
         local = t;
         return *j;
     }
@@ -529,13 +532,21 @@ struct OzJobTable {
     const int64_t *start;  // [n + 1]: first tile of each job, then the total
     int n;
     __device__ int64_t tiles() const { return start[n]; }
-    __device__ const OzJob &job(int64_t t, int64_t &local) const {
-        int lo = 0, hi = n - 1;  // the last job with start <= t
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) / 2;
-            if (start[mid] <= t) lo = mid;
-            else hi = mid - 1;
+    __device__ const OzJob &job(int64_t t, int64_t &local, int &hint) const {
+        int lo = hint;  // the last job with start <= t, at or after the hint
+        if (lo + 1 < n && start[lo + 1] <= t) {
+            ++lo;
+            if (lo + 1 < n && start[lo + 1] <= t) {
+                int hi = n - 1;
+                ++lo;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) / 2;
+                    if (start[mid] <= t) lo = mid;
+                    else hi = mid - 1;
+                }
+            }
         }
+        hint = lo;
         local = t - start[lo];
         return jobs[lo];
     }
@@ -544,17 +555,27 @@ struct OzJobTable {
 // Tile `local` of a job: batch entry, then grouped rasterisation within the
 // entry, so that consecutive tiles walk a band of `band` row tiles across all
 // column tiles and the CTAs resident at the same time share slices in L2.
+template <typename I>
+__device__ __forceinline__ void oz_tile_t(I local, I nn, I nm, I gm, int bn, int64_t &m0, int64_t &n0, int &l) {
+    const I per = nn * nm;
+    const I ll = local / per;
+    const I t = local - ll * per;
+    const I band = t / (gm * nn);
+    const I first = band * gm;
+    const I rows = min(gm, nm - first);
+    const I r = t - band * gm * nn;
+    l = (int)ll;
+    m0 = (int64_t)(first + r % rows) * OZ_BM;
+    n0 = (int64_t)(r / rows) * bn;
+}
 __device__ __forceinline__ void oz_tile(const OzJob &J, int64_t local, int bn, int64_t &m0, int64_t &n0, int &l) {
-    const int64_t nn = J.tiles_n, nm = J.tiles_m, per = nn * nm;
-    l = (int)(local / per);
-    const int64_t t = local - (int64_t)l * per;
-    const int64_t gm = J.a.band;
-    const int64_t band = t / (gm * nn);
-    const int64_t first = band * gm;
-    const int64_t rows = min(gm, nm - first);
-    const int64_t r = t - band * gm * nn;
-    m0 = (first + r % rows) * OZ_BM;
-    n0 = (r / rows) * bn;
+    const int64_t nn = J.tiles_n, nm = J.tiles_m, gm = J.a.band;
+    // 32-bit divisions whenever the job's tile numbers fit (a 64-bit division
+    // is a long software sequence)
+    if (local <= INT32_MAX && (int64_t)J.L * nn * nm <= INT32_MAX && gm * nn <= INT32_MAX)
+        oz_tile_t<uint32_t>((uint32_t)local, (uint32_t)nn, (uint32_t)nm, (uint32_t)gm, bn, m0, n0, l);
+    else
+        oz_tile_t<int64_t>(local, nn, nm, gm, bn, m0, n0, l);
 }
 
 // One CTA computes 128 x BN tiles of the embedded output, in turn for the
@@ -624,7 +645,8 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
     int32_t *status;
     {
         int64_t unused;
-        status = src.job(0, unused).a.status;
+        int h0 = 0;
+        status = src.job(0, unused, h0).a.status;
     }
 
     if (tid == 0) {
@@ -669,9 +691,10 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
         if (lane == 0) {
             uint32_t g = 0;  // k blocks issued so far, over all tiles of this CTA
             bool ok = true;
+            int hint = 0;
             for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
                 int64_t local;
-                const OzJob &J = src.job(t, local);
+                const OzJob &J = src.job(t, local, hint);
                 int64_t m0, n0;
                 int l;
                 oz_tile(J, local, BN, m0, n0, l);
@@ -704,9 +727,10 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
             const int me = warp == 1 ? 0 : 1;
             bool ok = true;
             uint32_t g = 0, C = 0;
+            int hint = 0;
             for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
                 int64_t local;
-                const OzJob &J = src.job(t, local);
+                const OzJob &J = src.job(t, local, hint);
                 const int nkb = J.a.nkb, kcb = J.a.kcb;
                 for (int c0 = 0; c0 < nkb && ok; c0 += kcb, ++C) {
                     const uint32_t bank = C & 1u;
@@ -751,9 +775,10 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
         const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16) + HALF * h;
         bool ok = true;
         uint32_t C = 0;  // chunks read so far, over all tiles of this CTA
+        int hint = 0;
         for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
             int64_t local;
-            const OzJob &J = src.job(t, local);
+            const OzJob &J = src.job(t, local, hint);
             const OzGemmArgs &args = J.a;
             int64_t m0, n0;
             int l;
