@@ -64,6 +64,7 @@ def parse():
                          "workload at --n / the permutation of A(a,b,c,d,e) with e = --perm-e (profiling cases); "
                          "hadamard / unary: broadcast product / partial sums of a 4.3 GB array")
     ap.add_argument("--form", default="ozaki", help="form of --workload kernel")
+    ap.add_argument("--band", type=int, default=0, help="rasterisation band of --workload kernel (0: default)")
     ap.add_argument("--perm-e", type=int, default=32, help="extent of label e in --workload permute")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="per offered rate in the serving sweep")
     ap.add_argument("--instances", type=int, default=4096)
@@ -531,7 +532,7 @@ def config2_bench(dev, steps=3):
     return res
 
 
-def kernel_case(dev, n, form, slices, steps, warmup):
+def kernel_case(dev, n, form, slices, steps, warmup, band=0):
     """One contraction of the precision workload at M = N = n (K = 8192),
     launched warmup + steps times; phase timing from the plan."""
     import ctypes
@@ -553,6 +554,7 @@ def kernel_case(dev, n, form, slices, steps, warmup):
     lib = _lib.load()
     st = torch.cuda.current_stream(dev).cuda_stream
     lib.mgb_plan_set_timing(p.handle, 1)
+    _lib.check(lib.mgb_plan_set_band(p.handle, band), lib)
     pre, main = [], []
     for r in range(warmup + steps):
         _lib.check(lib.mgb_contract(p.handle, A.data_ptr(), B.data_ptr(), C.data_ptr(), ws.data_ptr(), ws.numel(),
@@ -563,7 +565,7 @@ def kernel_case(dev, n, form, slices, steps, warmup):
             pre.append(fp.value)
             main.append(fm.value)
     ms = statistics.mean(main)
-    return {"n": n, "form": form, "slices": slices, "prepass_ms": statistics.mean(pre), "main_ms": ms,
+    return {"n": n, "form": form, "slices": slices, "band": band, "prepass_ms": statistics.mean(pre), "main_ms": ms,
             "tflops_alg": p.flops / ((statistics.mean(pre) + ms) / 1e3) / 1e12, "status": m.device_status(dev)}
 
 
@@ -716,7 +718,7 @@ def main():
             res = config2_bench(dev)
             metric = "plain vs emulated TFLOP/s on permuting shapes; permutation kernel GB/s"
         elif args.workload == "kernel":
-            res = kernel_case(dev, args.n, args.form, args.slices, args.steps, args.warmup)
+            res = kernel_case(dev, args.n, args.form, args.slices, args.steps, args.warmup, args.band)
             metric = "one contraction of the precision workload (profiling case)"
         elif args.workload == "permute":
             res = permute_case(dev, args.perm_e, args.steps, args.warmup)

@@ -129,6 +129,11 @@ int mgb_plan_info_get(mgb_plan plan, mgb_plan_info *info);
  * is enabled, execute the plan from one thread and one stream at a time. */
 int mgb_plan_set_timing(mgb_plan plan, int32_t enable);
 int mgb_plan_timing(mgb_plan plan, float *prepass_ms, float *main_ms);
+/* Rasterisation band of the emulated forms' tensor-core kernel: the number
+ * of row tiles (1..64) that consecutive tiles walk across all column tiles;
+ * 0 = the library's default. Changes the schedule only, never the result.
+ * No counterpart in the reference. */
+int mgb_plan_set_band(mgb_plan plan, int32_t band);
 int mgb_plan_workspace_size(mgb_plan plan, uint64_t *bytes);
 int mgb_plan_destroy(mgb_plan plan);
 

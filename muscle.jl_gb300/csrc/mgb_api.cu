@@ -413,6 +413,13 @@ int mgb_plan_set_timing(mgb_plan plan, int32_t enable) {
     return MGB_OK;
 }
 
+int mgb_plan_set_band(mgb_plan plan, int32_t band) {
+    if (!plan || plan->kind != PlanKind::Contraction) return fail(MGB_ERR_ARGUMENT, "band: not a contraction plan");
+    if (band < 0 || band > 64) return fail(MGB_ERR_ARGUMENT, "band must be in 0..64");
+    plan->cp.band = band;
+    return MGB_OK;
+}
+
 int mgb_plan_timing(mgb_plan plan, float *prepass_ms, float *main_ms) {
     if (!plan || !prepass_ms || !main_ms) return fail(MGB_ERR_ARGUMENT, "null argument");
     if (!plan->timing || !plan->ev[0]) return fail(MGB_ERR_ARGUMENT, "timing was not enabled");

@@ -72,8 +72,14 @@ constexpr int OZ_EPI_WARPS = 8;
 // Row tiles per rasterisation band. The resident CTAs drift apart in k over
 // many waves, so L2 keeps a band's A slices only while they are small: on the
 // 8192^3 ComplexF64 case (S = 6) DRAM traffic per launch is 222 GB for bands
-// of 1, 135 GB for 2, 124 GB for 3, 145 GB for 4 and 187-224 GB for 8.
+// of 1, 135 GB for 2, 124 GB for 3, 145 GB for 4 and 187-224 GB for 8. The
+// default is the widest band up to 3 whose A slices (band x 128 rows x all
+// of K x S slices) stay within OZ_BAND_BYTES: on the same case S = 8 (two
+// stages, so exposed to every L2 miss) ran 173 ms with bands of 3 (96 MiB),
+// 133 ms with 2 and 142 ms with 1, while S = 6 (72 MiB at 3) ran 76.0 ms
+// with 3 and 78.0 ms with 2.
 constexpr int OZ_GROUP_M = 3;
+constexpr int64_t OZ_BAND_BYTES = 90ll << 20;  // S = 7 at K_e = 16384: 84 MiB; S = 8: 96 MiB
 // warp 0 TMA, warp 1 MMA issuer (and TMEM owner), warps 2..9 epilogue,
 // warp 10 second MMA issuer
 constexpr int OZ_THREADS = 96 + 32 * OZ_EPI_WARPS;
@@ -1217,7 +1223,12 @@ static int ozaki_job(const ContractionPlan &p, void *C, void *ws, OzJob &job, in
     a.expB = exact ? (int32_t *)(w + p.ws_scale_b) : nullptr;
     a.C = C;
     a.cptr = p.pc;
-    a.band = p.band > 0 ? p.band : OZ_GROUP_M;
+    if (p.band > 0) {
+        a.band = p.band;
+    } else {
+        a.band = OZ_GROUP_M;
+        while (a.band > 1 && (int64_t)a.band * OZ_BM * p.kpad * S * 2 > OZ_BAND_BYTES) --a.band;
+    }
     a.gm = p.gm;
     a.gn = p.gn;
     a.gl = p.gl;

@@ -89,6 +89,7 @@ SIGNATURES = {
     "mgb_plan_workspace_size": (_i32, [_vp, _P(_u64)]),
     "mgb_plan_destroy": (_i32, [_vp]),
     "mgb_plan_set_timing": (_i32, [_vp, _i32]),
+    "mgb_plan_set_band": (_i32, [_vp, _i32]),
     "mgb_plan_timing": (_i32, [_vp, _P(ctypes.c_float), _P(ctypes.c_float)]),
     "mgb_group_create": (_i32, [_P(_vp), _P(_vp), _i32, _P(_vp), _P(_vp), _P(_vp)]),
     "mgb_group_update": (_i32, [_vp, _P(_vp), _P(_vp), _P(_vp)]),
