@@ -324,10 +324,10 @@ __device__ __forceinline__ uint32_t bf16_bits_of_int(int d) {
 }
 __device__ __forceinline__ uint32_t pack2(uint32_t lo, uint32_t hi) { return lo | (hi << 16); }
 
-// Signed round-to-nearest digits of x * 2^(-e) in 62-bit fixed point.
-__device__ __forceinline__ void oz_digits(double x, int e, int S, int W, int (&d)[8]) {
-    uint64_t b = (uint64_t)__double_as_longlong(x);
-    int be = (int)((b >> 52) & 0x7FF);
+// x * 2^(62 - e) truncated to a signed 62-bit fixed-point integer (|x| < 2^e).
+__device__ __forceinline__ int64_t oz_fixed(double x, int e) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const int be = (int)((b >> 52) & 0x7FF);
     int64_t m = (int64_t)(b & 0xFFFFFFFFFFFFFull);
     int ex;
     if (be) {
@@ -336,19 +336,19 @@ __device__ __forceinline__ void oz_digits(double x, int e, int S, int W, int (&d
     } else {
         ex = -1074;
     }
-    int sh = ex + 62 - e;  // Q = m * 2^sh < 2^62
+    const int sh = ex + 62 - e;  // Q = m * 2^sh < 2^62
     int64_t Q;
     if (sh >= 0) Q = m << sh;
     else if (sh > -63) Q = m >> (-sh);
     else Q = 0;
-    if (b >> 63) Q = -Q;
-#pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        int shift = 62 - W * (s + 1);
-        int64_t dig = (Q + ((int64_t)1 << (shift - 1))) >> shift;
-        Q -= dig << shift;
-        d[s] = s < S ? (int)dig : 0;
-    }
+    return (b >> 63) ? -Q : Q;
+}
+// The next signed digit of Q at weight 2^shift, rounded to nearest, taken out
+// of Q (the digits are produced most significant first).
+__device__ __forceinline__ int oz_take_digit(int64_t &Q, int shift) {
+    const int64_t dig = (Q + ((int64_t)1 << (shift - 1))) >> shift;
+    Q -= dig << shift;
+    return (int)dig;
 }
 
 // Three bf16 pieces of a float: x = hi + mid + lo (to ~2^-24 relative).
@@ -392,7 +392,7 @@ struct OzIn<float2> {
 
 // BF3 = true: float inputs split into bf16 pieces; otherwise Ozaki digits.
 template <typename T, int MODE, bool BF3>
-__global__ void __launch_bounds__(256) k_oz_slice(const T *__restrict__ X, OpGeom g,
+__global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, OpGeom g,
                                                   const int32_t *__restrict__ exps, int S, int W,
                                                   uint32_t *__restrict__ out, int64_t rows_e,
                                                   int64_t kw) {
@@ -432,63 +432,70 @@ __global__ void __launch_bounds__(256) k_oz_slice(const T *__restrict__ X, OpGeo
     __syncthreads();
     const int64_t plane = rows_e * kw;
     uint32_t *outl = out + l * (int64_t)S * plane;
+    // Each digit (or piece) plane is written as soon as it is known, so a
+    // thread holds two fixed-point values rather than arrays of digits.
     for (int j = 0; j < 4; ++j) {
         int r = ty + 8 * j;
         int64_t row = r0 + r;
         if (row >= g.R) continue;
         int e = BF3 ? 0 : rexp[r];
         bool bad = !BF3 && e == 0x7FFFFFFF;
+        if (bad) e = 0;
         if (MODE == MODE_REAL) {
             int64_t word = k0 / 2 + tx;
             if (word >= kw) continue;
-            uint32_t p0[8], p1[8];
+            uint32_t *o = outl + row * kw + word;
             if (BF3) {
+                uint32_t p0[8], p1[8];
                 bf3_pieces((float)OzIn<T>::re(tile[r][2 * tx]), p0);
                 bf3_pieces((float)OzIn<T>::re(tile[r][2 * tx + 1]), p1);
-            } else {
-                int d0[8], d1[8];
-                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx]), bad ? 0 : e, S, W, d0);
-                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx + 1]), bad ? 0 : e, S, W, d1);
 #pragma unroll
-                for (int s = 0; s < 8; ++s) {
-                    p0[s] = bf16_bits_of_int(d0[s]);
-                    p1[s] = bf16_bits_of_int(d1[s]);
+                for (int s = 0; s < 3; ++s) o[s * plane] = pack2(p0[s], p1[s]);
+            } else {
+                int64_t q0 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx]), e);
+                int64_t q1 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx + 1]), e);
+#pragma unroll 1
+                for (int s = 0; s < S; ++s, o += plane) {
+                    const int shift = 62 - W * (s + 1);
+                    const int d0 = oz_take_digit(q0, shift), d1 = oz_take_digit(q1, shift);
+                    *o = pack2(bf16_bits_of_int(d0), bf16_bits_of_int(d1));
                 }
             }
-#pragma unroll
-            for (int s = 0; s < 8; ++s)
-                if (s < S) outl[s * plane + row * kw + word] = pack2(p0[s], p1[s]);
         } else {
             int64_t word = k0 + tx;
             if (word >= kw) continue;
-            uint32_t pr[8], pi[8], pn[8];
+            // MODE_CA: row r; MODE_CB: rows 2r (re, -im) and 2r + 1 (im, re)
+            uint32_t *o = outl + (MODE == MODE_CB ? 2 * row : row) * kw + word;
             if (BF3) {
+                uint32_t pr[8], pi[8], pn[8];
                 bf3_pieces((float)OzIn<T>::re(tile[r][tx]), pr);
                 bf3_pieces((float)OzIn<T>::im(tile[r][tx]), pi);
                 float nim = -(float)OzIn<T>::im(tile[r][tx]);
                 bf3_pieces(nim, pn);
-            } else {
-                int dr[8], di[8];
-                oz_digits(bad ? 0.0 : (double)OzIn<T>::re(tile[r][tx]), bad ? 0 : e, S, W, dr);
-                oz_digits(bad ? 0.0 : (double)OzIn<T>::im(tile[r][tx]), bad ? 0 : e, S, W, di);
 #pragma unroll
-                for (int s = 0; s < 8; ++s) {
-                    pr[s] = bf16_bits_of_int(dr[s]);
-                    pi[s] = bf16_bits_of_int(di[s]);
-                    pn[s] = bf16_bits_of_int(-di[s]);
-                }
-            }
-            if (MODE == MODE_CA) {
-#pragma unroll
-                for (int s = 0; s < 8; ++s)
-                    if (s < S) outl[s * plane + row * kw + word] = pack2(pr[s], pi[s]);
-            } else {
-#pragma unroll
-                for (int s = 0; s < 8; ++s)
-                    if (s < S) {
-                        outl[s * plane + (2 * row) * kw + word] = pack2(pr[s], pn[s]);
-                        outl[s * plane + (2 * row + 1) * kw + word] = pack2(pi[s], pr[s]);
+                for (int s = 0; s < 3; ++s) {
+                    if (MODE == MODE_CA) {
+                        o[s * plane] = pack2(pr[s], pi[s]);
+                    } else {
+                        o[s * plane] = pack2(pr[s], pn[s]);
+                        o[s * plane + kw] = pack2(pi[s], pr[s]);
                     }
+                }
+            } else {
+                int64_t qr = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(tile[r][tx]), e);
+                int64_t qi = oz_fixed(bad ? 0.0 : (double)OzIn<T>::im(tile[r][tx]), e);
+#pragma unroll 1
+                for (int s = 0; s < S; ++s, o += plane) {
+                    const int shift = 62 - W * (s + 1);
+                    const int dr = oz_take_digit(qr, shift), di = oz_take_digit(qi, shift);
+                    const uint32_t br = bf16_bits_of_int(dr), bi = bf16_bits_of_int(di);
+                    if (MODE == MODE_CA) {
+                        *o = pack2(br, bi);
+                    } else {
+                        o[0] = pack2(br, bf16_bits_of_int(-di));
+                        o[kw] = pack2(bi, br);
+                    }
+                }
             }
         }
     }
