@@ -99,6 +99,29 @@ def test_plan_errors_map_to_julia_exceptions():
     assert st == _lib.ERR_ARGUMENT
 
 
+def test_plan_band_setting():
+    """The rasterisation band is a schedule knob: 0 (default) .. 64 row tiles,
+    rejected outside that range and on a null plan."""
+    from muscle_gb300 import _lib
+
+    lib = _lib.load()
+    da, _ = _lib.make_desc(*desc(_lib.C64, [0, 1], [300, 40]))
+    db, _ = _lib.make_desc(*desc(_lib.C64, [1, 2], [40, 70]))
+    dc, _ = _lib.make_desc(*desc(_lib.C64, [0, 2], [300, 70]))
+    h = ctypes.c_void_p()
+    assert lib.mgb_contraction_plan(ctypes.byref(h), ctypes.byref(da), ctypes.byref(db), ctypes.byref(dc),
+                                    _lib.FORM_OZAKI, 6) == 0
+    try:
+        for band in (0, 1, 2, 64):
+            assert lib.mgb_plan_set_band(h, band) == 0, band
+        for band in (-1, 65):
+            assert lib.mgb_plan_set_band(h, band) == _lib.ERR_ARGUMENT, band
+            assert b"band" in lib.mgb_last_error()
+    finally:
+        lib.mgb_plan_destroy(h)
+    assert lib.mgb_plan_set_band(None, 1) == _lib.ERR_ARGUMENT
+
+
 def test_plan_batch_and_scalar():
     from muscle_gb300 import _lib
 
