@@ -55,6 +55,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <cmath>
 #include <mutex>
@@ -1051,25 +1052,32 @@ static int make_map(CUtensorMap *tm, void *base, int64_t k_e, int64_t rows, int6
     return MGB_OK;
 }
 
+// Per-device caches, safe for concurrent callers: the values are idempotent,
+// so a race only repeats the query or the attribute call.
+constexpr int OZ_MAX_DEVICES = 64;
+
 static int sm_count() {
-    static int count[64] = {};
+    static std::atomic<int> count[OZ_MAX_DEVICES];
     int dev = 0;
     cudaGetDevice(&dev);
-    if (!count[dev & 63]) {
-        int n = 0;
+    const bool cached = dev >= 0 && dev < OZ_MAX_DEVICES;
+    int n = cached ? count[dev].load(std::memory_order_relaxed) : 0;
+    if (n <= 0) {
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        count[dev & 63] = n > 0 ? n : 1;
+        if (n <= 0) n = 1;
+        if (cached) count[dev].store(n, std::memory_order_relaxed);
     }
-    return count[dev & 63];
+    return n;
 }
 
 template <typename K>
-static int set_smem_attr(K kern, int smem, bool (&done)[64]) {
+static int set_smem_attr(K kern, int smem, std::atomic<bool> (&done)[OZ_MAX_DEVICES]) {
     int dev = 0;
     cudaGetDevice(&dev);
-    if (!done[dev & 63]) {
+    const bool cached = dev >= 0 && dev < OZ_MAX_DEVICES;
+    if (!cached || !done[dev].load(std::memory_order_acquire)) {
         MGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        done[dev & 63] = true;
+        if (cached) done[dev].store(true, std::memory_order_release);
     }
     return MGB_OK;
 }
@@ -1080,7 +1088,7 @@ template <int S, bool EXACT, bool CX>
 static int launch_gemm_t(const OzJob &job, int64_t tiles, cudaStream_t s) {
     auto kern = k_oz_gemm<S, EXACT, CX>;
     constexpr int smem = oz_smem_bytes(S, EXACT);
-    static bool attr_set[64] = {};
+    static std::atomic<bool> attr_set[OZ_MAX_DEVICES];
     if (int st = set_smem_attr(kern, smem, attr_set)) return st;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count());
     kern<<<grid, OZ_THREADS, smem, s>>>(job);
@@ -1092,7 +1100,7 @@ template <int S, bool EXACT, bool CX>
 static int launch_grouped_t(const OzJob *jobs, const int64_t *start, int njobs, int64_t tiles, cudaStream_t s) {
     auto kern = k_oz_gemm_grouped<S, EXACT, CX>;
     constexpr int smem = oz_smem_bytes(S, EXACT);
-    static bool attr_set[64] = {};
+    static std::atomic<bool> attr_set[OZ_MAX_DEVICES];
     if (int st = set_smem_attr(kern, smem, attr_set)) return st;
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, sm_count());
     kern<<<grid, OZ_THREADS, smem, s>>>(jobs, start, njobs);
