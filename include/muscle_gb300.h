@@ -143,8 +143,11 @@ int mgb_plan_destroy(mgb_plan plan);
  * launch per kernel, the batch index selecting the member's operand and
  * output pointers from a device array; other members run one by one. The
  * group copies the pointer arrays at creation into device memory;
- * mgb_group_update replaces them (a CUDA-graph replay of mgb_group_execute
- * then reads the new pointers). Operand pointers are device pointers.
+ * mgb_group_update replaces them with a synchronous copy (a CUDA-graph
+ * replay of mgb_group_execute then reads the new pointers): call it when no
+ * execution of the group is in flight. Operand pointers are device pointers.
+ * Device state that a captured graph launches with (pointer arrays, job
+ * tables) stays valid until mgb_group_destroy.
  * The ensemble of a PEPS sweep is the motivating case
  * (ext/MuscleDaggerExt/binary_einsum.jl:64-119 runs such independent pairs
  * as separate tasks).                                                      */

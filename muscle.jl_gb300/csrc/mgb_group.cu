@@ -50,6 +50,9 @@ struct mgb_group_s {
     // workspace moves.
     void *grouped_ws = nullptr;
     std::vector<mgb::OzGrouped *> grouped;
+    // Tables of earlier builds: a CUDA graph captured before the rebuild may
+    // still launch with them, so they live until the group is destroyed.
+    std::vector<mgb::OzGrouped *> retired;
 };
 
 using namespace mgb;
@@ -78,7 +81,9 @@ static int upload(mgb_group g) {
 
 static void free_grouped(mgb_group g) {
     for (auto *x : g->grouped) ozaki_grouped_destroy(x);
+    for (auto *x : g->retired) ozaki_grouped_destroy(x);
     g->grouped.clear();
+    g->retired.clear();
     g->grouped_ws = nullptr;
 }
 
@@ -92,7 +97,9 @@ static void free_group(mgb_group g) {
 // Job tables of the persistent GEMM launches, one per kernel variant
 // (slices, form, real or complex) of the emulated buckets.
 static int build_grouped(mgb_group g, void *workspace) {
-    free_grouped(g);
+    g->retired.insert(g->retired.end(), g->grouped.begin(), g->grouped.end());
+    g->grouped.clear();
+    g->grouped_ws = nullptr;
     std::map<std::tuple<int, int, int>, std::pair<std::vector<const ContractionPlan *>, std::vector<void *>>> sets;
     for (auto &b : g->buckets) {
         if (b.cp.form == MGB_FORM_PLAIN) continue;
@@ -103,7 +110,8 @@ static int build_grouped(mgb_group g, void *workspace) {
     for (auto &kv : sets) {
         OzGrouped *x = nullptr;
         if (int st = ozaki_grouped_create(kv.second.first, kv.second.second, &x)) {
-            free_grouped(g);
+            for (auto *y : g->grouped) ozaki_grouped_destroy(y);  // never launched
+            g->grouped.clear();
             return st;
         }
         g->grouped.push_back(x);
