@@ -8,9 +8,11 @@ on `(DomainCUDA, ...)` operands (the rule tables of
 src/Operations/binary_einsum.jl:20-31, src/Operations/unary_einsum.jl:20-24
 and src/Operations/hadamard.jl:4-5); the methods `ccall` into
 `libmuscle_gb300.so` (C ABI in include/muscle_gb300.h).
-`with_backend(f, BackendGB300(...))` selects a form explicitly. `Server` is
-the serving loop: contractions submitted as they arrive, admitted against a
-device-memory budget and batched onto several streams.
+`with_backend(f, BackendGB300(...))` selects a form explicitly. `Group` runs
+many independent contractions (a PEPS sweep's site pairs) as a few batched
+launches on one stream. `Server` is the serving loop: contractions submitted
+as they arrive, admitted against a device-memory budget and batched onto
+several streams.
 """
 module MuscleGB300
 
@@ -18,7 +20,7 @@ using CUDA
 using Muscle
 using Muscle: Backend, DomainCUDA, Index, Tensor, inds
 
-export BackendGB300, Server, submit!
+export BackendGB300, Server, submit!, Group, execute!
 
 const libmgb = get(ENV, "MUSCLE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libmuscle_gb300.so"))
 
@@ -231,6 +233,102 @@ function Base.close(srv::Server)
     end
     empty!(srv.plans)
     srv.handle = C_NULL
+    return nothing
+end
+
+# ---------------------------------------------------------------------------
+# Grouped contractions (mgb_group_*): independent c = a * b on one stream.
+# Members with equal plans (same shapes, strides, element types and form)
+# share one plan handle and run as one batched launch per kernel; the
+# emulated buckets' tensor-core work runs as one persistent launch per kernel
+# variant. ext/MuscleDaggerExt/binary_einsum.jl:64-119 runs such pairs as
+# separate tasks.
+
+devptr(t::Tensor) = Ptr{Cvoid}(reinterpret(UInt64, pointer(parent(t))))
+
+"""
+    Group(items; backend=BackendGB300())
+
+`items`: `(c, a, b)` tensor triples, labels as in `binary_einsum!`.
+`execute!(g)` computes every `c` on the current stream. After one
+`execute!`, the call can be captured into a CUDA graph and replayed; the
+device state it launches with stays valid until `close(g)`. The tensors must
+stay alive, at the same addresses, as long as the group.
+"""
+mutable struct Group
+    handle::Ptr{Cvoid}
+    plans::Vector{Ptr{Cvoid}}  # distinct plans, destroyed with the group
+    items::Vector{Any}
+    workspace::Union{CuArray{UInt8,1},Nothing}
+    nbytes::UInt64
+end
+
+function Group(items; backend::BackendGB300=BackendGB300())
+    cache = Dict{Any,Ptr{Cvoid}}()
+    members = Ptr{Cvoid}[]
+    g = Group(C_NULL, Ptr{Cvoid}[], collect(Any, items), nothing, UInt64(0))
+    finalizer(close, g)
+    for (c, a, b) in g.items
+        m = modemap(a, b, c)
+        aa, ab, ac = descarrays(a, m), descarrays(b, m), descarrays(c, m)
+        key = (eltype(a), eltype(b), eltype(c), aa, ab, ac)
+        plan = get(cache, key, C_NULL)
+        if plan == C_NULL
+            ref = Ref{Ptr{Cvoid}}(C_NULL)
+            GC.@preserve aa ab ac begin
+                da, db, dc = Ref(desc(a, aa)), Ref(desc(b, ab)), Ref(desc(c, ac))
+                check(ccall((:mgb_contraction_plan, libmgb), Cint,
+                            (Ptr{Ptr{Cvoid}}, Ref{TensorDesc}, Ref{TensorDesc}, Ref{TensorDesc}, Cint, Cint),
+                            ref, da, db, dc, backend.form, backend.slices))
+            end
+            plan = cache[key] = ref[]
+            push!(g.plans, plan)
+        end
+        push!(members, plan)
+    end
+    A = Ptr{Cvoid}[devptr(a) for (c, a, b) in g.items]
+    B = Ptr{Cvoid}[devptr(b) for (c, a, b) in g.items]
+    C = Ptr{Cvoid}[devptr(c) for (c, a, b) in g.items]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:mgb_group_create, libmgb), Cint,
+                (Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Cint, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}),
+                h, members, Cint(length(members)), A, B, C))
+    g.handle = h[]
+    bytes = Ref{UInt64}(0)
+    check(ccall((:mgb_group_workspace_size, libmgb), Cint, (Ptr{Cvoid}, Ref{UInt64}), g.handle, bytes))
+    g.nbytes = bytes[]
+    g.workspace = bytes[] == 0 ? nothing : CuArray{UInt8}(undef, bytes[])
+    return g
+end
+
+function execute!(g::Group)
+    ws = g.workspace === nothing ? CU_NULL : pointer(g.workspace)
+    check(ccall((:mgb_group_execute, libmgb), Cint, (Ptr{Cvoid}, CuPtr{Cvoid}, UInt64, CUDA.CUstream),
+                g.handle, ws, g.nbytes, CUDA.stream()))
+    return g
+end
+
+"""
+    set_bands!(g, bands)
+
+Rasterisation band per member: an index 0..5 into {1, 2, 3, 4, 8, 16} row
+tiles (any other value: the library's default). A schedule choice only.
+"""
+function set_bands!(g::Group, bands::AbstractVector{<:Integer})
+    length(bands) == length(g.items) || throw(ArgumentError("one band per member"))
+    check(ccall((:mgb_group_set_tiles, libmgb), Cint, (Ptr{Cvoid}, Ptr{Cint}), g.handle, Cint.(bands)))
+    return g
+end
+
+function Base.close(g::Group)
+    if g.handle != C_NULL
+        ccall((:mgb_group_destroy, libmgb), Cint, (Ptr{Cvoid},), g.handle)
+        g.handle = C_NULL
+    end
+    for plan in g.plans
+        ccall((:mgb_plan_destroy, libmgb), Cint, (Ptr{Cvoid},), plan)
+    end
+    empty!(g.plans)
     return nothing
 end
 
