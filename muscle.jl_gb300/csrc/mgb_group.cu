@@ -306,10 +306,8 @@ int mgb_group_execute(mgb_group group, void *workspace, uint64_t workspace_bytes
 
 int mgb_group_execute_part(mgb_group group, int32_t part, int32_t nparts, void *workspace, uint64_t workspace_bytes,
                            void *stream) {
-    if (!group) return fail(MGB_ERR_ARGUMENT, "group: null argument");
+    if (int st = check_ws(group, workspace, workspace_bytes)) return st;
     if (nparts < 1 || part < 0 || part >= nparts) return fail(MGB_ERR_ARGUMENT, "group: part out of range");
-    if (workspace_bytes < group->ws_bytes || (group->ws_bytes && !workspace))
-        return fail(MGB_ERR_WORKSPACE, "group workspace smaller than mgb_group_workspace_size");
     cudaStream_t s = (cudaStream_t)stream;
     if (nparts == 1) {
         const int nu = (int)(group->buckets.size() + group->singles.size());
