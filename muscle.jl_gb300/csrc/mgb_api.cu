@@ -9,10 +9,10 @@
 //    path supports (test/integration/cuda.jl:126-145);
 //  * result eltype = promote_eltype(a, b) (ext/MuscleCUDAExt.jl:16);
 //  * repeated labels must have equal extents (src/Tensor.jl:20-24).
+#include <atomic>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <numeric>
 
 #include "mgb_internal.h"
@@ -25,18 +25,20 @@ static thread_local std::string g_last_error;
 // and cleared by mgb_device_status(). Its address is looked up once per device.
 __device__ int32_t mgb_status_word;
 
+// Lock-free: the lookup is idempotent, so concurrent first calls at worst
+// repeat it, and later launches take no lock.
 int32_t *device_status_ptr() {
-    static std::mutex mu;
-    static int32_t *ptrs[128] = {};
+    static std::atomic<int32_t *> ptrs[128];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return nullptr;
-    std::lock_guard<std::mutex> lk(mu);
-    if (!ptrs[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, mgb_status_word) != cudaSuccess) return nullptr;
-        ptrs[dev] = (int32_t *)p;
+    int32_t *p = ptrs[dev].load(std::memory_order_acquire);
+    if (!p) {
+        void *q = nullptr;
+        if (cudaGetSymbolAddress(&q, mgb_status_word) != cudaSuccess) return nullptr;
+        p = (int32_t *)q;
+        ptrs[dev].store(p, std::memory_order_release);
     }
-    return ptrs[dev];
+    return p;
 }
 
 void set_error(const std::string &msg) { g_last_error = msg; }

@@ -20,7 +20,7 @@
 //  * the first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
 //    before any stream capture.
-#include <mutex>
+#include <atomic>
 
 #include "mgb_internal.h"
 
@@ -31,20 +31,19 @@ static __device__ __align__(256) unsigned char mgb_noalloc_scratch[MGB_NOALLOC_S
 
 // Device address of the array per device (host code cannot use the symbol as
 // a pointer: on the host it only names a stand-in object).
+// Lock-free per-device cache (the lookup is idempotent).
 int scratch_address(void **out) {
-    static std::mutex mu;
-    static void *addr[128] = {};
+    static std::atomic<void *> addr[128];
     int dev = 0;
     MGB_CUDA_CHECK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 128) return mgb::fail(MGB_ERR_CUDA, "device ordinal out of range");
-    std::lock_guard<std::mutex> lk(mu);
-    if (!addr[dev]) {
-        void *p = nullptr;
+    void *p = addr[dev].load(std::memory_order_acquire);
+    if (!p) {
         cudaError_t e = cudaGetSymbolAddress(&p, mgb_noalloc_scratch);
         if (e != cudaSuccess) return mgb::cuda_fail(e, "cudaGetSymbolAddress(mgb_noalloc_scratch)");
-        addr[dev] = p;
+        addr[dev].store(p, std::memory_order_release);
     }
-    *out = addr[dev];
+    *out = p;
     return MGB_OK;
 }
 
