@@ -34,8 +34,9 @@
 // B_e[2n+q][2k+p] holds [[Br, -Bi], [Bi, Br]] so that C_e[m][2n+q] is part q
 // of C[m,n] (4 real products per complex product, as zgemm's 4M form).
 //
-// Pipeline per CTA (128 x BN embedded outputs, BN = 32, or 64 for BF16X3;
-// one CTA per SM):
+// Pipeline per CTA (128 x BN embedded outputs per tile, BN = 32, or 64 for
+// BF16X3; a persistent grid of one CTA per SM, each walking the tiles b,
+// b + grid, ... of one contraction or of a group's job table):
 //   warp 0       TMA producer: one 3-D box per operand per 32-wide k block
 //                loads all S slices at once into a 64B-swizzled stage;
 //   warp 1       TMEM allocation, then one thread issues, per 16 k, one
