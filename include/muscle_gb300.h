@@ -73,7 +73,7 @@ typedef struct mgb_plan_s *mgb_plan;
 typedef struct mgb_plan_info {
     int64_t m, n, k, batch;   /* folded GEMM view: left, right, contracted, hyper */
     int32_t form;             /* resolved mgb_form                               */
-    int32_t slices;           /* Ozaki slice count (0 when not emulated)         */
+    int32_t slices;           /* Ozaki slice count (0: not emulated, or adaptive) */
     int32_t compute_dtype;    /* promoted element type of the result             */
     int32_t permute_a, permute_b, permute_c; /* 1 when PLAIN stages a permute     */
     double flops;             /* algorithmic: 8MNK complex, 2MNK real (x batch)  */
@@ -86,7 +86,16 @@ typedef struct mgb_plan_info {
  * (hyper) mode; a mode in exactly one operand and C is free. Any other pattern
  * is MGB_ERR_ARGUMENT. The result element type is promote_eltype(A, B)
  * (ext/MuscleCUDAExt.jl:16) and C must have it. alpha = 1, beta = 0.
- * slices: Ozaki slice count (0 = default 7); ignored by other forms.       */
+ * slices: Ozaki slice count 3..8, or 0 = adaptive (AUTO and OZAKI forms of
+ * a Float64 / ComplexF64 result): every mgb_contract then measures the
+ * operands on the device (per-row and per-column exponents, and the norms
+ * that bound the digit truncation and the dropped digit pairs) and runs the
+ * smallest slice count whose estimated relative Frobenius error is within
+ * the plan's tolerance (1e-13 unless mgb_plan_set_tolerance changed it), or
+ * the plain FP64 form when none is, e.g. for operands with Inf or NaN. The
+ * choice happens on the device: the call stays asynchronous and can be
+ * captured in a CUDA graph, each replay choosing again for its data. The
+ * workspace is sized for the largest candidate. Ignored by other forms.   */
 int mgb_contraction_plan(mgb_plan *plan, const mgb_tensor_desc *a,
                          const mgb_tensor_desc *b, const mgb_tensor_desc *c,
                          int32_t form, int32_t slices);
@@ -134,6 +143,25 @@ int mgb_plan_timing(mgb_plan plan, float *prepass_ms, float *main_ms);
  * 0 = the library's default. Changes the schedule only, never the result.
  * No counterpart in the reference. */
 int mgb_plan_set_band(mgb_plan plan, int32_t band);
+/* Target relative Frobenius error (> 0) of an adaptive plan's slice choice;
+ * the default 1e-13 is the tolerance Muscle.jl's Float64 results are held
+ * to. Set it before executing the plan, not while executions are in flight.
+ * MGB_ERR_ARGUMENT for plans that are not adaptive. No counterpart in the
+ * reference. */
+int mgb_plan_set_tolerance(mgb_plan plan, double tolerance);
+/* The choice of the last mgb_contract of an adaptive plan that ran with
+ * `workspace`, read from that workspace after synchronising `stream`.
+ * estimate[S] is the estimated relative Frobenius error with S slices for
+ * every candidate S (0 elsewhere); slices is the chosen count, 0 when the
+ * plain form ran. No counterpart in the reference.                       */
+typedef struct mgb_adaptive_report {
+    int32_t slices;        /* chosen slice count; 0: the plain FP64 form ran     */
+    int32_t nonfinite;     /* 1 when an operand holds Inf or NaN                  */
+    double estimate[9];    /* estimated relative error per candidate slice count */
+    double tolerance;      /* the plan's target                                   */
+} mgb_adaptive_report;
+int mgb_plan_adaptive_report(mgb_plan plan, const void *workspace, void *stream,
+                             mgb_adaptive_report *report);
 int mgb_plan_workspace_size(mgb_plan plan, uint64_t *bytes);
 int mgb_plan_destroy(mgb_plan plan);
 

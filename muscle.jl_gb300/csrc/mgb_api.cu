@@ -225,8 +225,12 @@ static int resolve_form(ContractionPlan &p, int form, int slices) {
         return fail(MGB_ERR_ARGUMENT, "unknown form");
     p.form = form;
     if (form == MGB_FORM_OZAKI) {
-        if (slices == 0) slices = 7;
-        if (slices < 3 || slices > 8) return fail(MGB_ERR_ARGUMENT, "OZAKI slices must be in 3..8");
+        if (slices == 0) {
+            p.adaptive = true;  // chosen per call from the operands (ozaki_setup sizes for the largest)
+            p.slices = 8;
+            return MGB_OK;
+        }
+        if (slices < 3 || slices > 8) return fail(MGB_ERR_ARGUMENT, "OZAKI slices must be in 3..8, or 0 (adaptive)");
         p.slices = slices;
     } else if (form == MGB_FORM_BF16X3) {
         p.slices = 3;
@@ -238,25 +242,11 @@ static int resolve_form(ContractionPlan &p, int form, int slices) {
 
 static uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
 
+// The plain kernels read operands of any element type in place (widening on
+// load), so the plain form needs no workspace.
 static void plain_workspace(ContractionPlan &p) {
-    p.convert_a = p.a.dtype != p.compute_dtype;
-    p.convert_b = p.b.dtype != p.compute_dtype;
-    uint64_t off = 0;
-    auto count = [](const Desc &d) {
-        int64_t n = 1;
-        for (int i = 0; i < d.rank; ++i) n *= d.ext[i];
-        return (uint64_t)n;
-    };
-    int eb = elem_bytes(p.compute_dtype);
-    if (p.convert_a) {
-        p.ws_a = off;
-        off = align256(off + count(p.a) * eb);
-    }
-    if (p.convert_b) {
-        p.ws_b = off;
-        off = align256(off + count(p.b) * eb);
-    }
-    p.ws_bytes = off;
+    p.convert_a = p.convert_b = false;
+    p.ws_bytes = 0;
 }
 
 }  // namespace mgb
@@ -285,6 +275,13 @@ int mgb_contraction_plan(mgb_plan *plan, const mgb_tensor_desc *a, const mgb_ten
     }
     if (cp.form == MGB_FORM_PLAIN) plain_workspace(cp);
     else ozaki_setup(cp);
+    if (cp.adaptive && cp.oz_R < 0) {  // no slice count holds K exactly: the plain form
+        cp.adaptive = false;
+        cp.form = MGB_FORM_PLAIN;
+        cp.slices = 0;
+        cp.oz_R = 0;
+        plain_workspace(cp);
+    }
     if (cp.oz_R < 0) {
         delete p;
         return fail(MGB_ERR_UNSUPPORTED, "contracted extent too long for the exact OZAKI accumulator");
@@ -322,7 +319,7 @@ int mgb_plan_info_get(mgb_plan plan, mgb_plan_info *info) {
     info->k = cp.K;
     info->batch = cp.L;
     info->form = cp.form;
-    info->slices = cp.form == MGB_FORM_OZAKI ? cp.slices : 0;
+    info->slices = (cp.form == MGB_FORM_OZAKI && !cp.adaptive) ? cp.slices : 0;
     info->compute_dtype = cp.compute_dtype;
     info->permute_a = cp.convert_a;
     info->permute_b = cp.convert_b;
@@ -366,46 +363,7 @@ static int contract_impl(mgb_plan plan, const void *A, const void *B, void *C, v
     if (plan->timing) MGB_CUDA_CHECK(cudaEventRecord(plan->ev[1], s));
     if (cp.K == 0) return launch_fill_zero(C, nc, cp.c.dtype, cp.c, s);  // empty sum
     if (!A || !B) return fail(MGB_ERR_ARGUMENT, "null operand pointer");
-    if (cp.form == MGB_FORM_PLAIN) {
-        ContractionPlan q = cp;
-        const void *a = A, *b = B;
-        int st;
-        if (cp.convert_a) {
-            Desc dst = cp.a;
-            dst.dtype = cp.compute_dtype;
-            int64_t dense = 1;
-            for (int i = 0; i < dst.rank; ++i) {
-                dst.str[i] = dense;
-                dense *= dst.ext[i];
-            }
-            void *wa = (char *)workspace + cp.ws_a;
-            if ((st = launch_permute(cp.a, dst, A, wa, s))) return st;
-            q.a = dst;
-            ContractionPlan r = q;  // re-fold with the new strides
-            if ((st = build_contraction(r))) return st;
-            q.gm = r.gm; q.gk = r.gk; q.gl = r.gl; q.gn = r.gn;
-            a = wa;
-        }
-        if (cp.convert_b) {
-            Desc dst = cp.b;
-            dst.dtype = cp.compute_dtype;
-            int64_t dense = 1;
-            for (int i = 0; i < dst.rank; ++i) {
-                dst.str[i] = dense;
-                dense *= dst.ext[i];
-            }
-            void *wb = (char *)workspace + cp.ws_b;
-            if ((st = launch_permute(cp.b, dst, B, wb, s))) return st;
-            q.b = dst;
-            ContractionPlan r = q;
-            if ((st = build_contraction(r))) return st;
-            q.gm = r.gm; q.gk = r.gk; q.gl = r.gl; q.gn = r.gn;
-            b = wb;
-        }
-        q.a.dtype = q.b.dtype = cp.compute_dtype;
-        if (plan->timing) MGB_CUDA_CHECK(cudaEventRecord(plan->ev[1], s));
-        return launch_plain_gemm(q, a, b, C, s);
-    }
+    if (cp.form == MGB_FORM_PLAIN) return launch_plain_gemm(cp, A, B, C, s);
     return launch_ozaki(cp, A, B, C, workspace, s, plan->timing ? plan->ev[1] : nullptr);
 }
 
@@ -420,6 +378,18 @@ int mgb_plan_set_band(mgb_plan plan, int32_t band) {
     if (band < 0 || band > 64) return fail(MGB_ERR_ARGUMENT, "band must be in 0..64");
     plan->cp.band = band;
     return MGB_OK;
+}
+
+int mgb_plan_set_tolerance(mgb_plan plan, double tolerance) {
+    if (!plan || plan->kind != PlanKind::Contraction)
+        return fail(MGB_ERR_ARGUMENT, "tolerance: not a contraction plan");
+    return ozaki_set_tolerance(plan->cp, tolerance);
+}
+
+int mgb_plan_adaptive_report(mgb_plan plan, const void *workspace, void *stream, mgb_adaptive_report *report) {
+    if (!plan || !report || plan->kind != PlanKind::Contraction)
+        return fail(MGB_ERR_ARGUMENT, "adaptive report: null argument or not a contraction plan");
+    return ozaki_adaptive_report(plan->cp, workspace, (cudaStream_t)stream, report);
 }
 
 int mgb_plan_timing(mgb_plan plan, float *prepass_ms, float *main_ms) {

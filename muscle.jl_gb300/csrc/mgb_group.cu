@@ -7,9 +7,8 @@
 // device array instead of a batch stride. A PEPS sweep (thousands of pairs of
 // a handful of shape classes) therefore costs a handful of launches per
 // class, all on one stream, so the caller can capture the group in one CUDA
-// graph. Members that cannot be batched (a plain-form plan that converts its
-// operands, an empty contraction, a plan that is already batched) run one by
-// one through mgb_contract. The workspace is carved into per-bucket and
+// graph. Members that cannot be batched (an empty contraction, a plan that is
+// already batched) run one by one through mgb_contract. The workspace is carved into per-bucket and
 // per-member slices.
 #include <algorithm>
 #include <map>
@@ -60,7 +59,6 @@ using namespace mgb;
 static bool batchable(const mgb_plan p) {
     const ContractionPlan &cp = p->cp;
     if (cp.L != 1 || cp.K == 0 || cp.M * cp.N == 0) return false;
-    if (cp.form == MGB_FORM_PLAIN && (cp.convert_a || cp.convert_b)) return false;
     return true;
 }
 
@@ -102,7 +100,9 @@ static int build_grouped(mgb_group g, void *workspace) {
     g->grouped_ws = nullptr;
     std::map<std::tuple<int, int, int>, std::pair<std::vector<const ContractionPlan *>, std::vector<void *>>> sets;
     for (auto &b : g->buckets) {
-        if (b.cp.form == MGB_FORM_PLAIN) continue;
+        // plain buckets have no tensor-core part; adaptive ones choose their
+        // slice count on the device and run their own launches
+        if (b.cp.form == MGB_FORM_PLAIN || b.cp.adaptive) continue;
         auto &e = sets[std::make_tuple(b.cp.slices, b.cp.form, is_complex(b.cp.compute_dtype) ? 1 : 0)];
         e.first.push_back(&b.cp);
         e.second.push_back((char *)workspace + b.ws_off);
@@ -289,6 +289,9 @@ int mgb_group_finish(mgb_group group, void *workspace, uint64_t workspace_bytes,
         if (int st = build_grouped(group, workspace)) return st;
     for (auto *x : group->grouped)
         if (int st = ozaki_grouped_launch(x, s)) return st;
+    for (auto &b : group->buckets)
+        if (b.cp.adaptive)
+            if (int st = ozaki_gemm(b.cp, nullptr, nullptr, nullptr, (char *)workspace + b.ws_off, s)) return st;
     const int nb = (int)group->buckets.size(), nu = nb + (int)group->singles.size();
     for (int u = nb; u < nu; ++u)
         if (int st = run_unit(group, u, workspace, s)) return st;

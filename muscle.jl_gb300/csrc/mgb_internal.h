@@ -104,13 +104,23 @@ struct ContractionPlan {
     // Groups: tensor index 0 = A, 1 = B, 2 = C.
     ModeGroup gm, gn, gk, gl;
     int64_t M = 1, N = 1, K = 1, L = 1;
-    // Plain form: operands of a different element type than the compute type
-    // are converted into the workspace first (dense, same mode order).
+    // Kept for mgb_plan_info's permute flags: always false, since the plain
+    // kernels read operands of any element type in place.
     bool convert_a = false, convert_b = false;
     // Ozaki / bf16x3 parameters.
     int oz_w = 7;          // slice width in bits
     int oz_kc = 256;       // k-chunk (embedded elements) between exact readouts
     int oz_R = 0;          // -1 when K is too long for the exact accumulator
+    // Adaptive OZAKI (slices = 0 at plan creation): every call measures the
+    // operands and picks the smallest slice count in `cand_mask` (bit S)
+    // whose estimated relative Frobenius error is within `tol`, or the plain
+    // form when none is. `slices` then holds the largest candidate (the
+    // workspace is sized for it).
+    bool adaptive = false;
+    uint32_t cand_mask = 0;
+    double tol = 1e-13;
+    uint64_t ws_stat = 0;  // statistics and the choice (OzStats, then P and q arrays)
+    uint64_t ws_conv = 0;  // mixed real x complex operands widened to complex (adaptive only)
     // Grouped execution: per-batch-entry operand / output pointers (device
     // arrays of L pointers) replace the batch strides when set.
     const void *const *pa = nullptr, *const *pb = nullptr;
@@ -149,8 +159,10 @@ namespace mgb {
 // Kernel launchers (each returns an mgb_status).
 int launch_permute(const Desc &x, const Desc &y, const void *X, void *Y, cudaStream_t s);
 int launch_fill_zero(void *p, int64_t count, int dtype, const Desc &d, cudaStream_t s);
+// `sel` (nullable): a device word; the launch does nothing unless it holds 0
+// (the adaptive choice "plain").
 int launch_plain_gemm(const ContractionPlan &p, const void *A, const void *B, void *C,
-                      cudaStream_t s);
+                      cudaStream_t s, const int32_t *sel = nullptr);
 int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C,
                  void *ws, cudaStream_t s, cudaEvent_t mid = nullptr);
 int launch_unary(const UnaryPlan &p, const void *X, void *Y, cudaStream_t s);
@@ -159,6 +171,13 @@ int selftest_wait_timeout(cudaStream_t s);
 // persistent GEMM launch for several plans of one kernel variant (same
 // slices, form and real/complex) whose slices lie in the given workspaces.
 int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *ws, cudaStream_t s);
+// The tensor-core part of one plan whose pre-pass has run into `ws` (for an
+// adaptive plan: one launch per candidate slice count, of which only the
+// chosen one works, and the plain form as the fallback).
+int ozaki_gemm(const ContractionPlan &p, const void *A, const void *B, void *C, void *ws, cudaStream_t s);
+// Reads the adaptive choice of the last call that ran with `ws` (synchronises s).
+int ozaki_adaptive_report(const ContractionPlan &p, const void *ws, cudaStream_t s, mgb_adaptive_report *out);
+int ozaki_set_tolerance(ContractionPlan &p, double tol);
 struct OzGrouped;
 int ozaki_grouped_create(const std::vector<const ContractionPlan *> &plans, const std::vector<void *> &ws,
                          OzGrouped **out);

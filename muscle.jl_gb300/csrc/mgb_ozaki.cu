@@ -270,8 +270,9 @@ __device__ __forceinline__ int bexp(double v) {
 __device__ __forceinline__ int bexp_of(double v) { return bexp(v); }
 __device__ __forceinline__ int bexp_of(double2 v) { return max(bexp(v.x), bexp(v.y)); }
 
+// `emax` (nullable): also the largest exponent of the whole operand.
 template <typename T>
-__global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps) {
+__global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps, int32_t *emax) {
     __shared__ int64_t roff[32], koff[32];
     __shared__ int red[8][33];
     int64_t tiles_k = (g.K + 31) / 32;
@@ -300,15 +301,179 @@ __global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeo
         }
     }
     __syncthreads();
-    if (tid < 32 && r0 + tid < g.R) {
+    if (tid < 32) {
         int e = 0;
-        if (g.rows_fast) {
-            for (int j = 0; j < 8; ++j) e = max(e, red[j][tid]);
-        } else {
-            e = red[tid / 8 % 4][tid];  // written by ty = tid % 8, j = tid / 8
+        if (r0 + tid < g.R) {
+            if (g.rows_fast) {
+                for (int j = 0; j < 8; ++j) e = max(e, red[j][tid]);
+            } else {
+                e = red[tid / 8 % 4][tid];  // written by ty = tid % 8, j = tid / 8
+            }
+            if (e > 0) atomicMax(exps + l * g.R + r0 + tid, e);
         }
-        if (e > 0) atomicMax(exps + l * g.R + r0 + tid, e);
+        if (emax) {
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, d));
+            if (tid == 0 && e > 0) atomicMax(emax, e);
+        }
     }
+}
+
+// =============================================================================
+// Adaptive slice count: operand statistics and the choice
+// =============================================================================
+// Error model of the OZAKI form with S digits of W bits (u = 2^-(W S)), for
+// row scales 2^e_i of A and column scales 2^f_j of B:
+//   * each scaled element is represented to within u/2 (round-to-nearest
+//     digits), an error of variance u^2/12 per real part: over C this sums to
+//     u^2/12 sum_ij (4^e_i |b_j|^2 + 4^f_j |a_i|^2) = u^2/12 (P_A Q_B + P_B Q_A)
+//     with P = sum of the squared scales and Q = squared Frobenius norm;
+//   * the dropped digit pairs (i + j = S, 0-based) are S - 1 products of
+//     digits of at most 2^(W-1) at weight 2^-(W (S+2)): variance at most
+//     (S - 1) u^2 / 144 per k per real product, (S - 1) u^2/144 K P_A P_B;
+//   * without cancellation, ||C||^2 = sum_k q_A[k] q_B[k] with q_A[k] the
+//     squared norm of A's column k and q_B[k] of B's row k.
+// Complex products count twice (re and im parts) in the first term and four
+// times in the second. A numpy emulation of the digit scheme gave estimate /
+// actual error between 1.0 (Gaussian data) and 5 (log-uniform magnitudes over
+// 2^-60..2^60) for every slice count. Everything is measured relative to the
+// operand's largest exponent, so the sums stay in float range.
+struct OzStats {
+    int32_t sel;        // chosen slice count, 0 = plain
+    int32_t nonfinite;  // an operand holds Inf / NaN
+    int32_t emax[2];    // largest biased exponent of A and B
+    float est[9];       // estimated error per candidate slice count
+    int32_t pad[3];
+};
+static_assert(sizeof(OzStats) == 64, "stats header");
+
+// 2^(2 d) as a float (0 below 2^-126)
+__device__ __forceinline__ float pow4f(int d) { return d >= -63 ? __int_as_float((127 + 2 * d) << 23) : 0.f; }
+
+// |x|^2 4^-(be_max + 1 - 1023), from the exponent and the top of the mantissa
+__device__ __forceinline__ float sq_rel(double x, int be_max) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const int be = (int)((b >> 52) & 0x7FF);
+    if (be == 0 || be == 0x7FF) return 0.f;  // zero / subnormal (negligible), non-finite (flagged)
+    const float f = __int_as_float(0x3F800000 | (uint32_t)((b >> 29) & 0x7FFFFF));
+    return f * f * pow4f(be - be_max - 1);
+}
+__device__ __forceinline__ float sq_rel(double2 x, int be_max) { return sq_rel(x.x, be_max) + sq_rel(x.y, be_max); }
+
+// Per k: q[l][k] += sum over the block's rows of |x|^2 relative to the
+// operand's largest exponent; the blocks of the first k tile also add the
+// rows' squared scales to P[l] and flag non-finite rows.
+template <typename T>
+__global__ void __launch_bounds__(256) k_oz_stat(const T *__restrict__ X, OpGeom g, const int32_t *__restrict__ exps,
+                                                 OzStats *st, int t, float *q, float *P) {
+    __shared__ int64_t roff[32], koff[32];
+    __shared__ float sq[32];
+    __shared__ float sp;
+    const int be_max = st->emax[t];
+    int64_t tiles_k = (g.K + 31) / 32;
+    int64_t tr = blockIdx.x / tiles_k, tk = blockIdx.x - tr * tiles_k;
+    int64_t l = blockIdx.y;
+    int64_t r0 = tr * 32, k0 = tk * 32;
+    int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
+    if (tid < 32) {
+        roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
+        sq[tid] = 0.f;
+        if (tid == 0) sp = 0.f;
+    } else if (tid < 64) {
+        koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
+    }
+    const T *Xl = g.ptrs ? (const T *)g.ptrs[l] : X + group_offset(g.gl, g.t, l);
+    __syncthreads();
+    if (g.rows_fast) {  // lanes walk rows: reduce over the warp per k
+        const int64_t r = r0 + tx;
+        for (int kk = ty; kk < 32; kk += 8) {
+            float v = (r < g.R && k0 + kk < g.K) ? sq_rel(__ldg(Xl + roff[tx] + koff[kk]), be_max) : 0.f;
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+            if (tx == 0) atomicAdd(&sq[kk], v);
+        }
+    } else {  // lanes walk k
+        float v = 0.f;
+        for (int j = 0; j < 4; ++j) {
+            const int rr = ty + 8 * j;
+            if (r0 + rr < g.R && k0 + tx < g.K) v += sq_rel(__ldg(Xl + roff[rr] + koff[tx]), be_max);
+        }
+        atomicAdd(&sq[tx], v);
+    }
+    if (tk == 0 && tid < 32) {
+        float w = 0.f;
+        if (r0 + tid < g.R) {
+            const int be = exps[l * g.R + r0 + tid];
+            if (be == 0x7FF) st->nonfinite = 1;
+            else if (be > 0) w = pow4f(be - be_max);
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) w += __shfl_xor_sync(0xffffffffu, w, d);
+        if (tid == 0) sp = w;
+    }
+    __syncthreads();
+    if (tid < 32 && k0 + tid < g.K && sq[tid] != 0.f) atomicAdd(q + l * g.K + k0 + tid, sq[tid]);
+    if (tid == 0 && tk == 0 && sp != 0.f) atomicAdd(P + l, sp);
+}
+
+// One block: the error estimate of every candidate slice count (bit S of
+// `cand`) and the choice, the smallest count within `tol`, else 0 (plain).
+__global__ void __launch_bounds__(1024) k_oz_choose(OzStats *st, const float *__restrict__ qa,
+                                                    const float *__restrict__ qb, const float *__restrict__ pa,
+                                                    const float *__restrict__ pb, int64_t K, int64_t L,
+                                                    uint32_t cand, double tol, double margin, int cx) {
+    __shared__ double red[3][32];
+    double trunc = 0.0, drop = 0.0, den = 0.0;
+    for (int64_t l = 0; l < L; ++l) {
+        double sa = 0.0, sb = 0.0, d = 0.0;
+        for (int64_t k = threadIdx.x; k < K; k += blockDim.x) {
+            const double x = qa[l * K + k], y = qb[l * K + k];
+            sa += x;
+            sb += y;
+            d += x * y;
+        }
+        const double Pa = pa[l], Pb = pb[l];
+        trunc += Pa * sb + Pb * sa;
+        den += d;
+        if (threadIdx.x == 0) drop += (double)K * Pa * Pb;
+    }
+    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        trunc += __shfl_xor_sync(0xffffffffu, trunc, o);
+        drop += __shfl_xor_sync(0xffffffffu, drop, o);
+        den += __shfl_xor_sync(0xffffffffu, den, o);
+    }
+    if (lane == 0) {
+        red[0][w] = trunc;
+        red[1][w] = drop;
+        red[2][w] = den;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    trunc = drop = den = 0.0;
+    for (int i = 0; i < (int)(blockDim.x + 31) / 32; ++i) {
+        trunc += red[0][i];
+        drop += red[1][i];
+        den += red[2][i];
+    }
+    const double f1 = cx ? 2.0 : 1.0, f2 = cx ? 4.0 : 1.0;
+    int sel = 0;
+    for (int S = 8; S >= 1; --S) {
+        st->est[S] = 0.f;
+        if (!(cand & (1u << S))) continue;
+        const int W = S <= 6 ? 8 : 7;
+        const double u = ldexp(1.0, -W * S);
+        const double num = u * u * (f1 / 12.0 * trunc + f2 * (S - 1) / 144.0 * drop);
+        double e;
+        if (num == 0.0) e = 0.0;                 // an operand is zero: every form is exact
+        else if (den == 0.0) e = INFINITY;       // no overlap the estimate can rest on
+        else e = sqrt(num / den) * margin;
+        st->est[S] = (float)e;
+        if (e <= tol && !st->nonfinite) sel = S;  // scanning down: ends at the smallest
+    }
+    st->est[0] = 0.f;
+    st->sel = sel;
 }
 
 // =============================================================================
@@ -393,11 +558,18 @@ struct OzIn<float2> {
 };
 
 // BF3 = true: float inputs split into bf16 pieces; otherwise Ozaki digits.
+// `sel` (nullable): the adaptive choice; the slice count is read from it and
+// the launch does nothing when it is 0 (plain).
 template <typename T, int MODE, bool BF3>
 __global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, OpGeom g,
                                                   const int32_t *__restrict__ exps, int S, int W,
                                                   uint32_t *__restrict__ out, int64_t rows_e,
-                                                  int64_t kw) {
+                                                  int64_t kw, const int32_t *__restrict__ sel) {
+    if (sel) {
+        S = *sel;
+        if (S == 0) return;
+        W = S <= 6 ? 8 : 7;
+    }
     constexpr int KT = MODE == MODE_REAL ? 64 : 32;  // k per tile
     __shared__ T tile[32][KT + 1];
     __shared__ int64_t roff[32], koff[KT];
@@ -518,6 +690,7 @@ struct OzGemmArgs {
     int32_t band;          // row tiles per rasterisation band
     ModeGroup gm, gn, gl;  // C offsets live in tensor slot 2
     int32_t *status;
+    const int32_t *sel;    // adaptive choice (nullable): run only when it holds S
 };
 
 // One contraction (or one bucket of a group) as the GEMM sees it: the slice
@@ -661,7 +834,11 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
     {
         int64_t unused;
         int h0 = 0;
-        status = src.job(0, unused, h0).a.status;
+        const OzGemmArgs &a0 = src.job(0, unused, h0).a;
+        // an adaptive plan launches every candidate; all but the chosen one
+        // return before touching shared memory or TMEM
+        if (a0.sel && *a0.sel != S) return;
+        status = a0.status;
     }
 
     if (tid == 0) {
@@ -992,8 +1169,34 @@ int selftest_wait_timeout(cudaStream_t s) {
 // =============================================================================
 static uint64_t align256(uint64_t x) { return (x + 255) & ~uint64_t(255); }
 
+// |X| <= k_e * 2^(2W) * 2^(W(S-1)) * (1 + small) must stay below 2^95.
+static bool oz_fits(int64_t k_e, int S) {
+    const int W = oz_digit_bits(S);
+    return std::log2((double)std::max<int64_t>(k_e, 1)) + 2 * W + W * (S - 1) + 1 < 94;
+}
+
+// Candidate slice counts of an adaptive plan: those whose exact accumulator
+// holds K and whose digits could reach the tolerance at all (2^-(W S) within
+// 64 tol; the estimate is at least about u for any data).
+static uint32_t oz_candidates(int64_t k_e, double tol) {
+    uint32_t m = 0;
+    for (int S = 3; S <= 8; ++S)
+        if (oz_fits(k_e, S) && std::ldexp(1.0, -oz_digit_bits(S) * S) <= 64.0 * tol) m |= 1u << S;
+    return m;
+}
+
 void ozaki_setup(ContractionPlan &p) {
     bool cx = is_complex(p.compute_dtype);
+    if (p.adaptive) {
+        const int64_t k_e = cx ? 2 * p.K : p.K;
+        p.cand_mask = oz_candidates(k_e, p.tol);
+        // the workspace holds the slices of the largest count that fits K, so
+        // that a later tolerance never needs more
+        p.slices = 0;
+        for (int S = 8; S >= 3 && !p.slices; --S)
+            if (oz_fits(k_e, S)) p.slices = S;
+        if (!p.slices) p.slices = 3;  // K too long for any count: ozaki_setup reports it below
+    }
     int S = p.slices;
     p.m_e = p.M;
     p.n_e = cx ? 2 * p.N : p.N;
@@ -1011,11 +1214,34 @@ void ozaki_setup(ContractionPlan &p) {
         off = align256(off + (uint64_t)p.L * p.M * 4);
         p.ws_scale_b = off;
         off = align256(off + (uint64_t)p.L * p.N * 4);
-        // |X| <= k_e * 2^(2W) * 2^(W(S-1)) * (1 + small) must stay below 2^95
-        double xb = std::log2((double)std::max<int64_t>(p.k_e, 1)) + 2 * p.oz_w + p.oz_w * (S - 1) + 1;
-        p.oz_R = xb < 94 ? 0 : -1;  // -1: K too long for the exact accumulator
+        p.oz_R = oz_fits(p.k_e, S) ? 0 : -1;  // -1: K too long for the exact accumulator
+        if (p.adaptive) {
+            // OzStats, P_A[L], P_B[L], q_A[L][K], q_B[L][K]
+            p.ws_stat = off;
+            off = align256(off + sizeof(OzStats) + 2 * (uint64_t)p.L * 4);
+            off = align256(off + 2 * (uint64_t)p.L * p.K * 4);
+        }
     }
     p.ws_bytes = off;
+}
+
+// Statistics area of an adaptive plan inside the workspace.
+struct OzStatArea {
+    OzStats *st;
+    float *pa, *pb, *qa, *qb;
+};
+static OzStatArea stat_area(const ContractionPlan &p, void *ws) {
+    OzStatArea a;
+    uint8_t *w = (uint8_t *)ws + p.ws_stat;
+    a.st = (OzStats *)w;
+    a.pa = (float *)(w + sizeof(OzStats));
+    a.pb = a.pa + p.L;
+    a.qa = (float *)((uint8_t *)ws + align256(p.ws_stat + sizeof(OzStats) + 2 * (uint64_t)p.L * 4));
+    a.qb = a.qa + p.L * p.K;
+    return a;
+}
+static uint64_t stat_bytes(const ContractionPlan &p) {
+    return align256(align256(sizeof(OzStats) + 2 * (uint64_t)p.L * 4) + 2 * (uint64_t)p.L * p.K * 4);
 }
 
 typedef CUresult (*PFN_encodeTiled_t)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -1144,27 +1370,39 @@ static int unit_row_fast(const ModeGroup &gr, const ModeGroup &gk, int t) {
 
 template <typename T, bool BF3>
 static int run_prepass(const OpGeom &g, int mode, const void *X, int32_t *exps, int S, uint32_t *out,
-                       int64_t rows_e, int64_t kw, int64_t L, cudaStream_t s) {
+                       int64_t rows_e, int64_t kw, int64_t L, cudaStream_t s, const int32_t *sel = nullptr) {
     int KT = mode == MODE_REAL ? 64 : 32;
     int64_t tiles = ((g.R + 31) / 32) * ((g.K + KT - 1) / KT);
     if (tiles > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the slicer grid");
     dim3 grid((unsigned)tiles, (unsigned)L);
     const T *x = (const T *)X;
     switch (mode) {
-    case MODE_REAL: k_oz_slice<T, MODE_REAL, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw); break;
-    case MODE_CA: k_oz_slice<T, MODE_CA, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw); break;
-    default: k_oz_slice<T, MODE_CB, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw); break;
+    case MODE_REAL: k_oz_slice<T, MODE_REAL, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw, sel); break;
+    case MODE_CA: k_oz_slice<T, MODE_CA, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw, sel); break;
+    default: k_oz_slice<T, MODE_CB, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw, sel); break;
     }
     MGB_CUDA_CHECK(cudaGetLastError());
     return MGB_OK;
 }
 
 template <typename T>
-static int run_scale(const OpGeom &g, const void *X, int32_t *exps, int64_t L, cudaStream_t s) {
+static int run_scale(const OpGeom &g, const void *X, int32_t *exps, int64_t L, cudaStream_t s,
+                     int32_t *emax = nullptr) {
     int64_t tiles = ((g.R + 31) / 32) * ((g.K + 31) / 32);
     if (tiles > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the scale grid");
     dim3 grid((unsigned)tiles, (unsigned)L);
-    k_oz_scale<T><<<grid, 256, 0, s>>>((const T *)X, g, exps);
+    k_oz_scale<T><<<grid, 256, 0, s>>>((const T *)X, g, exps, emax);
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
+}
+
+template <typename T>
+static int run_stat(const OpGeom &g, const void *X, const int32_t *exps, OzStats *st, int t, float *q, float *P,
+                    int64_t L, cudaStream_t s) {
+    int64_t tiles = ((g.R + 31) / 32) * ((g.K + 31) / 32);
+    if (tiles > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the statistics grid");
+    dim3 grid((unsigned)tiles, (unsigned)L);
+    k_oz_stat<T><<<grid, 256, 0, s>>>((const T *)X, g, exps, st, t, q, P);
     MGB_CUDA_CHECK(cudaGetLastError());
     return MGB_OK;
 }
@@ -1194,15 +1432,37 @@ int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *
     if (exact) {
         MGB_CUDA_CHECK(cudaMemsetAsync(ea, 0, (size_t)p.L * p.M * 4, s));
         MGB_CUDA_CHECK(cudaMemsetAsync(eb, 0, (size_t)p.L * p.N * 4, s));
-        st = p.a.dtype == MGB_C64 ? run_scale<double2>(ga, A, ea, p.L, s) : run_scale<double>(ga, A, ea, p.L, s);
+        OzStatArea sa_ = {};
+        const int32_t *sel = nullptr;
+        if (p.adaptive) {
+            sa_ = stat_area(p, ws);
+            MGB_CUDA_CHECK(cudaMemsetAsync(sa_.st, 0, stat_bytes(p), s));
+            sel = &sa_.st->sel;
+        }
+        int32_t *emax_a = p.adaptive ? &sa_.st->emax[0] : nullptr, *emax_b = p.adaptive ? &sa_.st->emax[1] : nullptr;
+        st = p.a.dtype == MGB_C64 ? run_scale<double2>(ga, A, ea, p.L, s, emax_a) : run_scale<double>(ga, A, ea, p.L, s, emax_a);
         if (st) return st;
-        st = p.b.dtype == MGB_C64 ? run_scale<double2>(gb, B, eb, p.L, s) : run_scale<double>(gb, B, eb, p.L, s);
+        st = p.b.dtype == MGB_C64 ? run_scale<double2>(gb, B, eb, p.L, s, emax_b) : run_scale<double>(gb, B, eb, p.L, s, emax_b);
         if (st) return st;
-        st = p.a.dtype == MGB_C64 ? run_prepass<double2, false>(ga, mode_a, A, ea, S, sa, p.m_e, kw, p.L, s)
-                                  : run_prepass<double, false>(ga, mode_a, A, ea, S, sa, p.m_e, kw, p.L, s);
+        if (p.adaptive) {
+            st = p.a.dtype == MGB_C64 ? run_stat<double2>(ga, A, ea, sa_.st, 0, sa_.qa, sa_.pa, p.L, s)
+                                      : run_stat<double>(ga, A, ea, sa_.st, 0, sa_.qa, sa_.pa, p.L, s);
+            if (st) return st;
+            st = p.b.dtype == MGB_C64 ? run_stat<double2>(gb, B, eb, sa_.st, 1, sa_.qb, sa_.pb, p.L, s)
+                                      : run_stat<double>(gb, B, eb, sa_.st, 1, sa_.qb, sa_.pb, p.L, s);
+            if (st) return st;
+            // Fluctuations of a Frobenius norm over few outputs: a margin that
+            // vanishes for large results.
+            const double margin = 1.0 + 2.0 / std::sqrt((double)std::max<int64_t>(p.M * p.N * p.L, 1));
+            k_oz_choose<<<1, 1024, 0, s>>>(sa_.st, sa_.qa, sa_.qb, sa_.pa, sa_.pb, p.K, p.L, p.cand_mask, p.tol,
+                                           margin, cx ? 1 : 0);
+            MGB_CUDA_CHECK(cudaGetLastError());
+        }
+        st = p.a.dtype == MGB_C64 ? run_prepass<double2, false>(ga, mode_a, A, ea, S, sa, p.m_e, kw, p.L, s, sel)
+                                  : run_prepass<double, false>(ga, mode_a, A, ea, S, sa, p.m_e, kw, p.L, s, sel);
         if (st) return st;
-        st = p.b.dtype == MGB_C64 ? run_prepass<double2, false>(gb, mode_b, B, eb, S, sb, p.n_e, kw, p.L, s)
-                                  : run_prepass<double, false>(gb, mode_b, B, eb, S, sb, p.n_e, kw, p.L, s);
+        st = p.b.dtype == MGB_C64 ? run_prepass<double2, false>(gb, mode_b, B, eb, S, sb, p.n_e, kw, p.L, s, sel)
+                                  : run_prepass<double, false>(gb, mode_b, B, eb, S, sb, p.n_e, kw, p.L, s, sel);
         if (st) return st;
     } else {
         st = p.a.dtype == MGB_C32 ? run_prepass<float2, true>(ga, mode_a, A, nullptr, 3, sa, p.m_e, kw, p.L, s)
@@ -1216,9 +1476,10 @@ int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *
 }
 
 // The GEMM's view of a plan whose slices lie in `ws`.
-static int ozaki_job(const ContractionPlan &p, void *C, void *ws, OzJob &job, int64_t &tiles) {
+static int ozaki_job(const ContractionPlan &p, void *C, void *ws, OzJob &job, int64_t &tiles, int S = 0,
+                     const int32_t *sel = nullptr) {
     const bool exact = p.form == MGB_FORM_OZAKI;
-    const int S = p.slices;
+    if (S == 0) S = p.slices;
     uint8_t *w = (uint8_t *)ws;
     uint32_t *sa = (uint32_t *)(w + p.ws_a), *sb = (uint32_t *)(w + p.ws_b);
     int32_t *status = device_status_ptr();
@@ -1249,6 +1510,7 @@ static int ozaki_job(const ContractionPlan &p, void *C, void *ws, OzJob &job, in
     a.gn = p.gn;
     a.gl = p.gl;
     a.status = status;
+    a.sel = sel;
     if (a.gm.n == 0) { a.gm.n = 1; a.gm.ext[0] = 1; for (int t = 0; t < 3; ++t) a.gm.str[t][0] = 0; }
     if (a.gn.n == 0) { a.gn.n = 1; a.gn.ext[0] = 1; for (int t = 0; t < 3; ++t) a.gn.str[t][0] = 0; }
     job.tiles_n = (int32_t)((p.n_e + bn - 1) / bn);
@@ -1260,15 +1522,53 @@ static int ozaki_job(const ContractionPlan &p, void *C, void *ws, OzJob &job, in
     return MGB_OK;
 }
 
+int ozaki_gemm(const ContractionPlan &p, const void *A, const void *B, void *C, void *ws, cudaStream_t s) {
+    int st;
+    OzJob job;
+    int64_t tiles = 0;
+    if (!p.adaptive) {
+        if ((st = ozaki_job(p, C, ws, job, tiles))) return st;
+        return launch_gemm(p.slices, p.form == MGB_FORM_OZAKI, is_complex(p.compute_dtype), job, tiles, s);
+    }
+    // Every candidate is launched; the kernel of the chosen count works and
+    // the others return at once. With no count chosen the plain form runs.
+    const int32_t *sel = &stat_area(p, ws).st->sel;
+    for (int S = 3; S <= 8; ++S) {
+        if (!(p.cand_mask & (1u << S))) continue;
+        if ((st = ozaki_job(p, C, ws, job, tiles, S, sel))) return st;
+        if ((st = launch_gemm(S, true, is_complex(p.compute_dtype), job, tiles, s))) return st;
+    }
+    return launch_plain_gemm(p, A, B, C, s, sel);
+}
+
 int launch_ozaki(const ContractionPlan &p, const void *A, const void *B, void *C, void *ws,
                  cudaStream_t s, cudaEvent_t mid) {
     int st = ozaki_prepass(p, A, B, ws, s);
     if (st) return st;
     if (mid) MGB_CUDA_CHECK(cudaEventRecord(mid, s));
-    OzJob job;
-    int64_t tiles = 0;
-    if ((st = ozaki_job(p, C, ws, job, tiles))) return st;
-    return launch_gemm(p.slices, p.form == MGB_FORM_OZAKI, is_complex(p.compute_dtype), job, tiles, s);
+    return ozaki_gemm(p, A, B, C, ws, s);
+}
+
+int ozaki_adaptive_report(const ContractionPlan &p, const void *ws, cudaStream_t s, mgb_adaptive_report *out) {
+    if (!p.adaptive) return fail(MGB_ERR_ARGUMENT, "adaptive report: the plan has a fixed slice count");
+    if (!ws) return fail(MGB_ERR_ARGUMENT, "adaptive report: null workspace");
+    OzStats h;
+    MGB_CUDA_CHECK(cudaMemcpyAsync(&h, stat_area(p, const_cast<void *>(ws)).st, sizeof(h), cudaMemcpyDeviceToHost, s));
+    MGB_CUDA_CHECK(cudaStreamSynchronize(s));
+    std::memset(out, 0, sizeof(*out));
+    out->slices = h.sel;
+    out->nonfinite = h.nonfinite;
+    for (int S = 0; S <= 8; ++S) out->estimate[S] = (p.cand_mask & (1u << S)) ? (double)h.est[S] : 0.0;
+    out->tolerance = p.tol;
+    return MGB_OK;
+}
+
+int ozaki_set_tolerance(ContractionPlan &p, double tol) {
+    if (!p.adaptive) return fail(MGB_ERR_ARGUMENT, "tolerance: the plan has a fixed slice count");
+    if (!(tol > 0.0)) return fail(MGB_ERR_ARGUMENT, "tolerance must be positive");
+    p.tol = tol;
+    p.cand_mask = oz_candidates(is_complex(p.compute_dtype) ? 2 * p.K : p.K, tol);
+    return MGB_OK;
 }
 
 // ---- one persistent GEMM launch for several plans of one kernel variant ----

@@ -8,6 +8,7 @@
 //  * Float32 / ComplexF32: FP32 FFMA on CUDA cores.
 // The FP64 pipe of GB300 is the roofline of this form.
 #include <algorithm>
+#include <type_traits>
 
 #include "mgb_internal.h"
 
@@ -20,6 +21,7 @@ struct GemmArgs {
     int64_t M, N, K;
     int a_kfast;  // A's unit-stride mode is contracted (else left)
     int b_kfast;  // B's unit-stride mode is contracted (else right)
+    const int32_t *sel;  // adaptive choice (nullable): run only when it holds 0
 };
 
 template <typename T>
@@ -61,8 +63,10 @@ __device__ __forceinline__ void dmma16816(double (&c)[4], const double (&a)[8], 
 constexpr int BM = 64, BN = 64, BK = 16, PADD = 4;
 
 // Tile loader shared by both kernels: fills sre/sim[k][r] (r = m or n) from an
-// operand whose row group is `gr` and contracted group `gk` (tensor t).
-template <typename T, typename R, int NT>
+// operand whose row group is `gr` and contracted group `gk` (tensor t). A
+// real operand of a complex contraction (promote_eltype, src/Muscle.jl:47)
+// is widened here, with zero imaginary parts (CXR: complex result).
+template <typename T, typename R, int NT, bool CXR>
 __device__ __forceinline__ void load_tile(const T *__restrict__ base, const int64_t *rowoff,
                                           const int64_t *koff, int64_t rows_left, int64_t k_left,
                                           int kfast, R (*sre)[BM + PADD], R (*sim)[BM + PADD]) {
@@ -78,27 +82,28 @@ __device__ __forceinline__ void load_tile(const T *__restrict__ base, const int6
         R vr = 0, vi = 0;
         if (r < rows_left && k < k_left) {
             T v = __ldg(base + rowoff[r] + koff[k]);
-            vr = Cx<T>::re(v);
-            vi = Cx<T>::im(v);
+            vr = (R)Cx<T>::re(v);
+            vi = (R)Cx<T>::im(v);
         }
         sre[k][r] = vr;
-        if (Cx<T>::complex) sim[k][r] = vi;
+        if (CXR) sim[k][r] = vi;
     }
 }
 
 // ---------------------------------------------------------------- DMMA (FP64)
-template <typename T>
-__global__ void __launch_bounds__(128) k_plain_dmma(const T *__restrict__ A, const T *__restrict__ B,
+template <typename TA, typename TB, typename T>
+__global__ void __launch_bounds__(128) k_plain_dmma(const TA *__restrict__ A, const TB *__restrict__ B,
                                                     T *__restrict__ C, GemmArgs g) {
     constexpr bool CX = Cx<T>::complex;
+    if (g.sel && *g.sel != 0) return;
     __shared__ double As_re[BK][BM + PADD], Bs_re[BK][BN + PADD];
     __shared__ double As_im[CX ? BK : 1][BM + PADD], Bs_im[CX ? BK : 1][BN + PADD];
     __shared__ int64_t rowA[BM], colB[BN], kA[BK], kB[BK];
 
     const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
     const int64_t l = blockIdx.z;
-    const T *Ab = g.pa ? (const T *)g.pa[l] : A + group_offset(g.gl, 0, l);
-    const T *Bb = g.pb ? (const T *)g.pb[l] : B + group_offset(g.gl, 1, l);
+    const TA *Ab = g.pa ? (const TA *)g.pa[l] : A + group_offset(g.gl, 0, l);
+    const TB *Bb = g.pb ? (const TB *)g.pb[l] : B + group_offset(g.gl, 1, l);
     T *Cb = g.pc ? (T *)g.pc[l] : C + group_offset(g.gl, 2, l);
     int tid = threadIdx.x;
     if (tid < BM) rowA[tid] = (m0 + tid < g.M) ? group_offset(g.gm, 0, m0 + tid) : 0;
@@ -120,9 +125,9 @@ __global__ void __launch_bounds__(128) k_plain_dmma(const T *__restrict__ A, con
         if (tid < BK) kA[tid] = (k0 + tid < g.K) ? group_offset(g.gk, 0, k0 + tid) : 0;
         else if (tid < 2 * BK) kB[tid - BK] = (k0 + tid - BK < g.K) ? group_offset(g.gk, 1, k0 + tid - BK) : 0;
         __syncthreads();
-        load_tile<T, double, 128>(Ab, rowA, kA, g.M - m0, g.K - k0, g.a_kfast, As_re, As_im);
+        load_tile<TA, double, 128, CX>(Ab, rowA, kA, g.M - m0, g.K - k0, g.a_kfast, As_re, As_im);
         // B rows are n: element (k, n) at colB[n] + kB[k]
-        load_tile<T, double, 128>(Bb, colB, kB, g.N - n0, g.K - k0, g.b_kfast, Bs_re, Bs_im);
+        load_tile<TB, double, 128, CX>(Bb, colB, kB, g.N - n0, g.K - k0, g.b_kfast, Bs_re, Bs_im);
         __syncthreads();
         double bre[4][4], bim[4][4];
 #pragma unroll
@@ -181,17 +186,18 @@ __global__ void __launch_bounds__(128) k_plain_dmma(const T *__restrict__ A, con
 }
 
 // ---------------------------------------------------------------- FFMA (FP32)
-template <typename T>
-__global__ void __launch_bounds__(256) k_plain_ffma(const T *__restrict__ A, const T *__restrict__ B,
+template <typename TA, typename TB, typename T>
+__global__ void __launch_bounds__(256) k_plain_ffma(const TA *__restrict__ A, const TB *__restrict__ B,
                                                     T *__restrict__ C, GemmArgs g) {
     constexpr bool CX = Cx<T>::complex;
+    if (g.sel && *g.sel != 0) return;
     __shared__ float As_re[BK][BM + PADD], Bs_re[BK][BN + PADD];
     __shared__ float As_im[CX ? BK : 1][BM + PADD], Bs_im[CX ? BK : 1][BN + PADD];
     __shared__ int64_t rowA[BM], colB[BN], kA[BK], kB[BK];
     const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
     const int64_t l = blockIdx.z;
-    const T *Ab = g.pa ? (const T *)g.pa[l] : A + group_offset(g.gl, 0, l);
-    const T *Bb = g.pb ? (const T *)g.pb[l] : B + group_offset(g.gl, 1, l);
+    const TA *Ab = g.pa ? (const TA *)g.pa[l] : A + group_offset(g.gl, 0, l);
+    const TB *Bb = g.pb ? (const TB *)g.pb[l] : B + group_offset(g.gl, 1, l);
     T *Cb = g.pc ? (T *)g.pc[l] : C + group_offset(g.gl, 2, l);
     int tid = threadIdx.x;
     if (tid < BM) rowA[tid] = (m0 + tid < g.M) ? group_offset(g.gm, 0, m0 + tid) : 0;
@@ -207,8 +213,8 @@ __global__ void __launch_bounds__(256) k_plain_ffma(const T *__restrict__ A, con
         if (tid < BK) kA[tid] = (k0 + tid < g.K) ? group_offset(g.gk, 0, k0 + tid) : 0;
         else if (tid < 2 * BK) kB[tid - BK] = (k0 + tid - BK < g.K) ? group_offset(g.gk, 1, k0 + tid - BK) : 0;
         __syncthreads();
-        load_tile<T, float, 256>(Ab, rowA, kA, g.M - m0, g.K - k0, g.a_kfast, As_re, As_im);
-        load_tile<T, float, 256>(Bb, colB, kB, g.N - n0, g.K - k0, g.b_kfast, Bs_re, Bs_im);
+        load_tile<TA, float, 256, CX>(Ab, rowA, kA, g.M - m0, g.K - k0, g.a_kfast, As_re, As_im);
+        load_tile<TB, float, 256, CX>(Bb, colB, kB, g.N - n0, g.K - k0, g.b_kfast, Bs_re, Bs_im);
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < BK; ++k) {
@@ -255,8 +261,45 @@ static int unit_stride_in(const ModeGroup &g, int t) {
     return g.n > 0 && (g.str[t][0] == 1 || g.str[t][0] == -1);
 }
 
+template <typename T>
+constexpr bool is_dbl() {
+    return std::is_same<T, double>::value || std::is_same<T, double2>::value;
+}
+// (TA, TB) -> T is Julia's promote_eltype over {Float32, Float64, ComplexF32, ComplexF64}
+template <typename TA, typename TB, typename T>
+constexpr bool promotes_to() {
+    return (Cx<TA>::complex || Cx<TB>::complex) == Cx<T>::complex && (is_dbl<TA>() || is_dbl<TB>()) == is_dbl<T>();
+}
+
+template <typename TA, typename TB, typename T>
+static void launch_typed(dim3 grid, const void *A, const void *B, void *C, const GemmArgs &g, cudaStream_t s) {
+    if constexpr (promotes_to<TA, TB, T>()) {
+        if constexpr (is_dbl<T>())
+            k_plain_dmma<TA, TB, T><<<grid, 128, 0, s>>>((const TA *)A, (const TB *)B, (T *)C, g);
+        else
+            k_plain_ffma<TA, TB, T><<<grid, 256, 0, s>>>((const TA *)A, (const TB *)B, (T *)C, g);
+    }
+}
+
+// Operand element type `d` as the kernels' load type.
+template <typename T>
+struct AsType {
+    typedef T type;
+};
+
+template <typename F>
+static bool with_type(int d, F &&f) {
+    switch (d) {
+    case MGB_F32: f(AsType<float>{}); return true;
+    case MGB_F64: f(AsType<double>{}); return true;
+    case MGB_C32: f(AsType<float2>{}); return true;
+    case MGB_C64: f(AsType<double2>{}); return true;
+    }
+    return false;
+}
+
 int launch_plain_gemm(const ContractionPlan &p, const void *A, const void *B, void *C,
-                      cudaStream_t s) {
+                      cudaStream_t s, const int32_t *sel) {
     GemmArgs g;
     g.gm = p.gm;
     g.gn = p.gn;
@@ -268,18 +311,33 @@ int launch_plain_gemm(const ContractionPlan &p, const void *A, const void *B, vo
     g.pa = p.pa;
     g.pb = p.pb;
     g.pc = p.pc;
+    g.sel = sel;
     g.a_kfast = unit_stride_in(p.gk, 0) && !unit_stride_in(p.gm, 0);
     g.b_kfast = unit_stride_in(p.gk, 1) && !unit_stride_in(p.gn, 1);
     int64_t gx = (p.N + BN - 1) / BN, gy = (p.M + BM - 1) / BM;
     if (gy > 65535) return fail(MGB_ERR_UNSUPPORTED, "plain: M too large for the grid");
     dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)p.L);
+    // Operands are read in their own element types (a real operand of a
+    // complex contraction, or Float32 in a Float64 one, is widened on load).
+    bool ok = false;
+    auto go = [&](auto tc) {
+        typedef typename decltype(tc)::type T;
+        with_type(p.a.dtype, [&](auto ta) {
+            typedef typename decltype(ta)::type TA;
+            with_type(p.b.dtype, [&](auto tb) {
+                typedef typename decltype(tb)::type TB;
+                launch_typed<TA, TB, T>(grid, A, B, C, g, s);
+                ok = promotes_to<TA, TB, T>();
+            });
+        });
+    };
     switch (p.compute_dtype) {
-    case MGB_F64: k_plain_dmma<double><<<grid, 128, 0, s>>>((const double *)A, (const double *)B, (double *)C, g); break;
-    case MGB_C64: k_plain_dmma<double2><<<grid, 128, 0, s>>>((const double2 *)A, (const double2 *)B, (double2 *)C, g); break;
-    case MGB_F32: k_plain_ffma<float><<<grid, 256, 0, s>>>((const float *)A, (const float *)B, (float *)C, g); break;
-    case MGB_C32: k_plain_ffma<float2><<<grid, 256, 0, s>>>((const float2 *)A, (const float2 *)B, (float2 *)C, g); break;
-    default: return fail(MGB_ERR_ARGUMENT, "plain: bad dtype");
+    case MGB_F64: go(AsType<double>{}); break;
+    case MGB_C64: go(AsType<double2>{}); break;
+    case MGB_F32: go(AsType<float>{}); break;
+    case MGB_C32: go(AsType<float2>{}); break;
     }
+    if (!ok) return fail(MGB_ERR_ARGUMENT, "plain: bad dtype");
     MGB_CUDA_CHECK(cudaGetLastError());
     return MGB_OK;
 }

@@ -23,6 +23,10 @@ ERR_DEVICE_TIMEOUT = 6
 ERR_OUT_OF_MEMORY = 7
 ERR_NOT_FINITE = 8
 
+# Size of the library's fixed scratch array behind mgb_contract_noalloc
+# (MGB_NOALLOC_SCRATCH_BYTES in the header; a host test keeps the two equal).
+NOALLOC_SCRATCH_BYTES = 32 << 20
+
 F32, F64, C32, C64 = 0, 1, 2, 3
 FORM_AUTO, FORM_PLAIN, FORM_OZAKI, FORM_BF16X3 = 0, 1, 2, 3
 
@@ -61,6 +65,15 @@ class PlanInfo(ctypes.Structure):
     ]
 
 
+class AdaptiveReport(ctypes.Structure):
+    _fields_ = [
+        ("slices", ctypes.c_int32),
+        ("nonfinite", ctypes.c_int32),
+        ("estimate", ctypes.c_double * 9),
+        ("tolerance", ctypes.c_double),
+    ]
+
+
 class ServerStats(ctypes.Structure):
     _fields_ = [
         ("submitted", ctypes.c_uint64),
@@ -91,6 +104,8 @@ SIGNATURES = {
     "mgb_plan_set_timing": (_i32, [_vp, _i32]),
     "mgb_plan_set_band": (_i32, [_vp, _i32]),
     "mgb_plan_timing": (_i32, [_vp, _P(ctypes.c_float), _P(ctypes.c_float)]),
+    "mgb_plan_set_tolerance": (_i32, [_vp, ctypes.c_double]),
+    "mgb_plan_adaptive_report": (_i32, [_vp, _vp, _vp, _P(AdaptiveReport)]),
     "mgb_group_create": (_i32, [_P(_vp), _P(_vp), _i32, _P(_vp), _P(_vp), _P(_vp)]),
     "mgb_group_update": (_i32, [_vp, _P(_vp), _P(_vp), _P(_vp)]),
     "mgb_group_workspace_size": (_i32, [_vp, _P(_u64)]),

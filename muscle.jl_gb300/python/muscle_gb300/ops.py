@@ -55,6 +55,27 @@ class Plan:
     def flops(self) -> float:
         return float(self.info.flops)
 
+    @property
+    def adaptive(self) -> bool:
+        """True for an OZAKI plan whose slice count is chosen per call."""
+        return self.info.form == _lib.FORM_OZAKI and self.info.slices == 0
+
+    def set_tolerance(self, tol: float) -> None:
+        """Target relative Frobenius error of an adaptive plan's choice."""
+        check(_lib.load().mgb_plan_set_tolerance(self.handle, float(tol)))
+
+    def report(self, workspace, stream=None) -> dict:
+        """The adaptive choice of the last call that ran with ``workspace``
+        (a device tensor or pointer): ``slices`` (0: the plain form ran),
+        ``estimate`` per candidate slice count, ``nonfinite``, ``tolerance``."""
+        lib = _lib.load()
+        r = _lib.AdaptiveReport()
+        wp = workspace.data_ptr() if hasattr(workspace, "data_ptr") else int(workspace)
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        check(lib.mgb_plan_adaptive_report(self.handle, wp, st, ctypes.byref(r)), lib)
+        return {"slices": int(r.slices), "nonfinite": bool(r.nonfinite), "tolerance": float(r.tolerance),
+                "estimate": {S: float(r.estimate[S]) for S in range(9) if r.estimate[S] > 0 or S == r.slices}}
+
     def __del__(self):
         try:
             if self.handle:
@@ -171,7 +192,9 @@ class BackendGB300(Backend):
     """The GB300 backend. ``form`` is one of "auto" (Ozaki for Float64 /
     ComplexF64 results, BF16x3 for Float32 / ComplexF32), "plain" (native
     FP64 DMMA / FP32 FFMA), "ozaki" or "bf16x3"; ``slices`` is the Ozaki
-    slice count (3..8, 0 = default 7)."""
+    slice count (3..8), or 0 (the default): chosen on the device for every
+    call, the smallest count whose estimated relative error is within 1e-13,
+    else the plain FP64 form."""
 
     def __init__(self, form: str = "auto", slices: int = 0):
         if form not in _lib.FORMS:

@@ -199,3 +199,47 @@ def test_front_end_label_algebra_matches_oracle(kat_cases):
             ix = [m.Index(x) for x in case["x"]["inds"]]
             got = unary_inds_y(ix, case["dims"], case["out"])
             assert [i.tag for i in got] == case["expect"]["inds"], case["name"]
+
+
+def test_noalloc_scratch_constant_matches_header():
+    """The Python constant the no-allocation tests size against is the
+    header's MGB_NOALLOC_SCRATCH_BYTES."""
+    import re
+
+    from muscle_gb300 import _lib
+
+    hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "muscle_gb300.h")).read()
+    m = re.search(r"#define MGB_NOALLOC_SCRATCH_BYTES \((\d+)u << (\d+)\)", hdr)
+    assert m, "MGB_NOALLOC_SCRATCH_BYTES not found"
+    assert _lib.NOALLOC_SCRATCH_BYTES == int(m.group(1)) << int(m.group(2))
+
+
+def test_adaptive_plan():
+    """slices = 0: an adaptive OZAKI plan (plan info reports slice count 0),
+    its workspace sized for the largest candidate, and a tolerance setter
+    that only adaptive plans accept."""
+    from muscle_gb300 import _lib
+
+    a, b, c = desc(_lib.C64, [0, 1], [512, 700]), desc(_lib.C64, [1, 2], [700, 300]), desc(_lib.C64, [0, 2], [512, 300])
+    st, info, _ = _plan(a, b, c, _lib.FORM_AUTO, 0)
+    assert st == 0 and info.form == _lib.FORM_OZAKI and info.slices == 0
+    assert info.workspace_bytes >= 8 * 512 * 1400 * 2 + 8 * 600 * 1400 * 2  # eight slices of A and B
+    st, fixed, _ = _plan(a, b, c, _lib.FORM_OZAKI, 6)
+    assert st == 0 and fixed.slices == 6 and fixed.workspace_bytes < info.workspace_bytes
+    lib = _lib.load()
+    da, ka = _lib.make_desc(*a)
+    db, kb = _lib.make_desc(*b)
+    dc, kc = _lib.make_desc(*c)
+    for slices, ok in ((0, True), (6, False)):
+        h = ctypes.c_void_p()
+        assert lib.mgb_contraction_plan(ctypes.byref(h), ctypes.byref(da), ctypes.byref(db), ctypes.byref(dc),
+                                        _lib.FORM_OZAKI, slices) == 0
+        assert (lib.mgb_plan_set_tolerance(h, 1e-10) == 0) == ok
+        if ok:
+            assert lib.mgb_plan_set_tolerance(h, 0.0) == _lib.ERR_ARGUMENT
+            assert lib.mgb_plan_set_tolerance(h, -1.0) == _lib.ERR_ARGUMENT
+        lib.mgb_plan_destroy(h)
+    # mixed element types need no workspace in the plain form
+    st, info, _ = _plan(desc(_lib.F64, [0, 1], [40, 50]), desc(_lib.C64, [1, 2], [50, 30]),
+                        desc(_lib.C64, [0, 2], [40, 30]), _lib.FORM_PLAIN, 0)
+    assert st == 0 and info.workspace_bytes == 0 and info.permute_a == 0

@@ -53,7 +53,9 @@ def test_noalloc_matches_workspace_entry_point_twice():
 
 
 def _lib_max():
-    return 32 << 20
+    from muscle_gb300 import _lib
+
+    return _lib.NOALLOC_SCRATCH_BYTES
 
 
 def test_noalloc_rejects_plans_larger_than_its_scratch():
