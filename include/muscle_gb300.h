@@ -171,9 +171,11 @@ int mgb_plan_destroy(mgb_plan plan);
  * launch per kernel, the batch index selecting the member's operand and
  * output pointers from a device array; other members run one by one. The
  * group copies the pointer arrays at creation into device memory;
- * mgb_group_update replaces them with a synchronous copy (a CUDA-graph
- * replay of mgb_group_execute then reads the new pointers): call it when no
- * execution of the group is in flight. Operand pointers are device pointers.
+ * mgb_group_update replaces them (a CUDA-graph replay of mgb_group_execute
+ * then reads the new pointers) after waiting for the executions and graph
+ * replays of the group already launched: every execution records an event
+ * on its stream, captured as an external event node in a graph. Operand
+ * pointers are device pointers.
  * Device state that a captured graph launches with (pointer arrays, job
  * tables) stays valid until mgb_group_destroy.
  * The ensemble of a PEPS sweep is the motivating case
@@ -272,8 +274,10 @@ int mgb_contract_noalloc(mgb_plan plan, const void *A, const void *B, void *C,
 
 /* ---- status ---------------------------------------------------------------*/
 const char *mgb_last_error(void);
-/* Reads and clears the device-side status word written by bounded waits and
- * non-finite checks of kernels launched on `stream` (synchronises it).     */
+/* Reads and clears, in one atomic exchange ordered on `stream`, the status
+ * word of the current device written by bounded waits of the library's
+ * kernels. The word is per device: it collects what kernels on every stream
+ * and host thread recorded. Synchronises `stream`.                         */
 int mgb_device_status(void *stream, int32_t *status);
 /* Self-test of the bounded device waits (no counterpart in the reference):
  * launches one CTA whose mbarrier wait nothing ever completes, through the

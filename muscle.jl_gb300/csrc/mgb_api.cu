@@ -23,7 +23,17 @@ static thread_local std::string g_last_error;
 
 // Device status word written by bounded waits of the tcgen05 kernels; read
 // and cleared by mgb_device_status(). Its address is looked up once per device.
-__device__ int32_t mgb_status_word;
+// One word per device, shared by every stream and host thread; it is
+// element 0 of the array, and the elements after it receive the values that
+// mgb_device_status exchanges out (a ring of slots, one per call, so that
+// concurrent callers on different streams do not share an output).
+constexpr int kStatusSlots = 64;
+__device__ int32_t mgb_status_word[1 + kStatusSlots];
+static std::atomic<uint32_t> g_status_slot{0};
+
+// Read-and-clear in one atomic exchange, so that a timeout recorded by a
+// kernel on another stream between a read and a clear cannot be lost.
+__global__ void k_status_exchange(int32_t *word, int32_t *out) { *out = atomicExch(word, 0); }
 
 // Lock-free: the lookup is idempotent, so concurrent first calls at worst
 // repeat it, and later launches take no lock.
@@ -503,13 +513,15 @@ int mgb_selftest_wait_timeout(void *stream) { return selftest_wait_timeout((cuda
 
 int mgb_device_status(void *stream, int32_t *status) {
     if (!status) return fail(MGB_ERR_ARGUMENT, "null status pointer");
-    MGB_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+    cudaStream_t s = (cudaStream_t)stream;
     int32_t *d = device_status_ptr();
     if (!d) return fail(MGB_ERR_CUDA, "device status word unavailable");
+    int32_t *out = d + 1 + (int)(g_status_slot.fetch_add(1, std::memory_order_relaxed) % kStatusSlots);
+    k_status_exchange<<<1, 1, 0, s>>>(d, out);
+    MGB_CUDA_CHECK(cudaGetLastError());
     int32_t v = 0;
-    MGB_CUDA_CHECK(cudaMemcpy(&v, d, sizeof(v), cudaMemcpyDeviceToHost));
-    int32_t zero = 0;
-    MGB_CUDA_CHECK(cudaMemcpy(d, &zero, sizeof(zero), cudaMemcpyHostToDevice));
+    MGB_CUDA_CHECK(cudaMemcpyAsync(&v, out, sizeof(v), cudaMemcpyDeviceToHost, s));
+    MGB_CUDA_CHECK(cudaStreamSynchronize(s));
     *status = v;
     return MGB_OK;
 }

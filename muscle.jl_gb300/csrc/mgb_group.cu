@@ -12,6 +12,7 @@
 // per-member slices.
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <tuple>
 #include <vector>
 
@@ -52,6 +53,11 @@ struct mgb_group_s {
     // Tables of earlier builds: a CUDA graph captured before the rebuild may
     // still launch with them, so they live until the group is destroyed.
     std::vector<mgb::OzGrouped *> retired;
+    // One event per stream an execution ran on, recorded at its end (inside a
+    // CUDA graph as an external event node, so replays record it too):
+    // mgb_group_update waits for them before it rewrites the pointer arrays.
+    std::vector<std::pair<cudaStream_t, cudaEvent_t>> done;
+    std::mutex done_mu;
 };
 
 using namespace mgb;
@@ -85,7 +91,27 @@ static void free_grouped(mgb_group g) {
     g->grouped_ws = nullptr;
 }
 
+// Records the end of an execution on `s` (see mgb_group_s::done).
+static int mark_done(mgb_group g, cudaStream_t s) {
+    cudaEvent_t ev = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g->done_mu);
+        for (auto &x : g->done)
+            if (x.first == s) ev = x.second;
+        if (!ev) {
+            MGB_CUDA_CHECK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            g->done.push_back({s, ev});
+        }
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    MGB_CUDA_CHECK(cudaStreamIsCapturing(s, &cap));
+    if (cap == cudaStreamCaptureStatusActive) MGB_CUDA_CHECK(cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal));
+    else MGB_CUDA_CHECK(cudaEventRecord(ev, s));
+    return MGB_OK;
+}
+
 static void free_group(mgb_group g) {
+    for (auto &x : g->done) cudaEventDestroy(x.second);
     free_grouped(g);
     for (auto &b : g->buckets)
         if (b.dptr) cudaFree(b.dptr);
@@ -193,6 +219,11 @@ int mgb_group_create(mgb_group *group, const mgb_plan *plans, int32_t count, con
 
 int mgb_group_update(mgb_group group, const void *const *A, const void *const *B, void *const *C) {
     if (!group || !A || !B || !C) return fail(MGB_ERR_ARGUMENT, "group: null argument");
+    {
+        // executions (and graph replays) still reading the pointer arrays
+        std::lock_guard<std::mutex> lk(group->done_mu);
+        for (auto &x : group->done) MGB_CUDA_CHECK(cudaEventSynchronize(x.second));
+    }
     for (size_t i = 0; i < group->plans.size(); ++i) {
         group->A[i] = A[i];
         group->B[i] = B[i];
@@ -274,12 +305,12 @@ int mgb_group_prepare_part(mgb_group group, int32_t part, int32_t nparts, void *
     if (nparts == 1) {
         for (int u = 0; u < nb; ++u)
             if (int st = one(u)) return st;
-        return MGB_OK;
+        return mark_done(group, s);
     }
     for (int u : part_units(group, part, nparts))
         if (u < nb)
             if (int st = one(u)) return st;
-    return MGB_OK;
+    return mark_done(group, s);
 }
 
 int mgb_group_finish(mgb_group group, void *workspace, uint64_t workspace_bytes, void *stream) {
@@ -295,7 +326,7 @@ int mgb_group_finish(mgb_group group, void *workspace, uint64_t workspace_bytes,
     const int nb = (int)group->buckets.size(), nu = nb + (int)group->singles.size();
     for (int u = nb; u < nu; ++u)
         if (int st = run_unit(group, u, workspace, s)) return st;
-    return MGB_OK;
+    return mark_done(group, s);
 }
 
 int mgb_group_execute(mgb_group group, void *workspace, uint64_t workspace_bytes, void *stream) {
@@ -316,11 +347,11 @@ int mgb_group_execute_part(mgb_group group, int32_t part, int32_t nparts, void *
         const int nu = (int)(group->buckets.size() + group->singles.size());
         for (int u = 0; u < nu; ++u)
             if (int st = run_unit(group, u, workspace, s)) return st;
-        return MGB_OK;
+        return mark_done(group, s);
     }
     for (int u : part_units(group, part, nparts))
         if (int st = run_unit(group, u, workspace, s)) return st;
-    return MGB_OK;
+    return mark_done(group, s);
 }
 
 int mgb_group_destroy(mgb_group group) {

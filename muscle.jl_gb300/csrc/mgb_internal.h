@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -178,6 +179,28 @@ int ozaki_gemm(const ContractionPlan &p, const void *A, const void *B, void *C, 
 // Reads the adaptive choice of the last call that ran with `ws` (synchronises s).
 int ozaki_adaptive_report(const ContractionPlan &p, const void *ws, cudaStream_t s, mgb_adaptive_report *out);
 int ozaki_set_tolerance(ContractionPlan &p, double tol);
+// Batched execution of different emulated-form contractions (each with its
+// own workspace `ws`, sized by its plan): one launch per pre-pass phase over
+// all operands, one chooser launch for the adaptive ones, and one persistent
+// tensor-core launch per kernel variant. `sel_dev_out` (device, one int32 per
+// item, nullable) receives each item's slice count (0: an adaptive item chose
+// the plain form, which the caller must then run). `after_prepass` is called
+// on the host once the pre-pass and `sel_dev_out` are queued and before any
+// tensor-core launch, `after_variant` after each variant's launch (slice
+// count, exact form, complex), e.g. to queue copies or record events.
+// Plain-form plans are rejected.
+struct OzBatchItem {
+    const ContractionPlan *p;
+    const void *A, *B;
+    void *C;
+    void *ws;
+};
+struct OzBatchBuffers;
+OzBatchBuffers *ozaki_batch_buffers_create();
+void ozaki_batch_buffers_destroy(OzBatchBuffers *b);
+int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *buf, cudaStream_t s,
+                       int32_t *sel_dev_out, const std::function<int()> &after_prepass,
+                       const std::function<int(int S, bool exact, bool cx)> &after_variant);
 struct OzGrouped;
 int ozaki_grouped_create(const std::vector<const ContractionPlan *> &plans, const std::vector<void *> &ws,
                          OzGrouped **out);

@@ -57,6 +57,10 @@
 
 #include <algorithm>
 #include <atomic>
+#include <functional>
+#include <map>
+#include <tuple>
+#include <type_traits>
 #include <cstring>
 #include <cmath>
 #include <mutex>
@@ -269,35 +273,41 @@ __device__ __forceinline__ int bexp(double v) {
 }
 __device__ __forceinline__ int bexp_of(double v) { return bexp(v); }
 __device__ __forceinline__ int bexp_of(double2 v) { return max(bexp(v.x), bexp(v.y)); }
+// Float32 operands of a Float64 / ComplexF64 contraction (promote_eltype),
+// widened exactly
+__device__ __forceinline__ int bexp_of(float v) { return bexp((double)v); }
+__device__ __forceinline__ int bexp_of(float2 v) { return max(bexp((double)v.x), bexp((double)v.y)); }
 
 // `emax` (nullable): also the largest exponent of the whole operand.
+struct ScaleSmem {
+    int64_t roff[32], koff[32];
+    int red[8][33];
+};
 template <typename T>
-__global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps, int32_t *emax) {
-    __shared__ int64_t roff[32], koff[32];
-    __shared__ int red[8][33];
+__device__ __forceinline__ void oz_scale_tile(const T *__restrict__ X, const OpGeom &g, int32_t *exps,
+                                              int32_t *emax, int64_t blk, int64_t l, ScaleSmem &sm) {
     int64_t tiles_k = (g.K + 31) / 32;
-    int64_t tr = blockIdx.x / tiles_k, tk = blockIdx.x - tr * tiles_k;
-    int64_t l = blockIdx.y;
+    int64_t tr = blk / tiles_k, tk = blk - tr * tiles_k;
     int64_t r0 = tr * 32, k0 = tk * 32;
     int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
-    if (tid < 32) roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
-    else if (tid < 64) koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
+    if (tid < 32) sm.roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
+    else if (tid < 64) sm.koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
     const T *Xl = g.ptrs ? (const T *)g.ptrs[l] : X + group_offset(g.gl, g.t, l);
     __syncthreads();
     if (g.rows_fast) {
         int e = 0;
         int64_t r = r0 + tx;
         for (int kk = ty; kk < 32; kk += 8)
-            if (r < g.R && k0 + kk < g.K) e = max(e, bexp_of(__ldg(Xl + roff[tx] + koff[kk])));
-        red[ty][tx] = e;
+            if (r < g.R && k0 + kk < g.K) e = max(e, bexp_of(__ldg(Xl + sm.roff[tx] + sm.koff[kk])));
+        sm.red[ty][tx] = e;
     } else {
         for (int j = 0; j < 4; ++j) {
             int rr = ty + 8 * j;
             int e = 0;
-            if (r0 + rr < g.R && k0 + tx < g.K) e = bexp_of(__ldg(Xl + roff[rr] + koff[tx]));
+            if (r0 + rr < g.R && k0 + tx < g.K) e = bexp_of(__ldg(Xl + sm.roff[rr] + sm.koff[tx]));
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, d));
-            if (tx == 0) red[j][rr] = e;  // rows rr = ty + 8 j are distinct per (ty, j)
+            if (tx == 0) sm.red[j][rr] = e;  // rows rr = ty + 8 j are distinct per (ty, j)
         }
     }
     __syncthreads();
@@ -305,9 +315,9 @@ __global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeo
         int e = 0;
         if (r0 + tid < g.R) {
             if (g.rows_fast) {
-                for (int j = 0; j < 8; ++j) e = max(e, red[j][tid]);
+                for (int j = 0; j < 8; ++j) e = max(e, sm.red[j][tid]);
             } else {
-                e = red[tid / 8 % 4][tid];  // written by ty = tid % 8, j = tid / 8
+                e = sm.red[tid / 8 % 4][tid];  // written by ty = tid % 8, j = tid / 8
             }
             if (e > 0) atomicMax(exps + l * g.R + r0 + tid, e);
         }
@@ -317,6 +327,11 @@ __global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeo
             if (tid == 0 && e > 0) atomicMax(emax, e);
         }
     }
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps, int32_t *emax) {
+    __shared__ ScaleSmem sm;
+    oz_scale_tile<T>(X, g, exps, emax, blockIdx.x, blockIdx.y, sm);
 }
 
 // =============================================================================
@@ -359,46 +374,50 @@ __device__ __forceinline__ float sq_rel(double x, int be_max) {
     return f * f * pow4f(be - be_max - 1);
 }
 __device__ __forceinline__ float sq_rel(double2 x, int be_max) { return sq_rel(x.x, be_max) + sq_rel(x.y, be_max); }
+__device__ __forceinline__ float sq_rel(float x, int be_max) { return sq_rel((double)x, be_max); }
+__device__ __forceinline__ float sq_rel(float2 x, int be_max) { return sq_rel((double)x.x, be_max) + sq_rel((double)x.y, be_max); }
 
 // Per k: q[l][k] += sum over the block's rows of |x|^2 relative to the
 // operand's largest exponent; the blocks of the first k tile also add the
 // rows' squared scales to P[l] and flag non-finite rows.
+struct StatSmem {
+    int64_t roff[32], koff[32];
+    float sq[32];
+    float sp;
+};
 template <typename T>
-__global__ void __launch_bounds__(256) k_oz_stat(const T *__restrict__ X, OpGeom g, const int32_t *__restrict__ exps,
-                                                 OzStats *st, int t, float *q, float *P) {
-    __shared__ int64_t roff[32], koff[32];
-    __shared__ float sq[32];
-    __shared__ float sp;
+__device__ __forceinline__ void oz_stat_tile(const T *__restrict__ X, const OpGeom &g,
+                                             const int32_t *__restrict__ exps, OzStats *st, int t, float *q,
+                                             float *P, int64_t blk, int64_t l, StatSmem &sm) {
     const int be_max = st->emax[t];
     int64_t tiles_k = (g.K + 31) / 32;
-    int64_t tr = blockIdx.x / tiles_k, tk = blockIdx.x - tr * tiles_k;
-    int64_t l = blockIdx.y;
+    int64_t tr = blk / tiles_k, tk = blk - tr * tiles_k;
     int64_t r0 = tr * 32, k0 = tk * 32;
     int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
     if (tid < 32) {
-        roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
-        sq[tid] = 0.f;
-        if (tid == 0) sp = 0.f;
+        sm.roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
+        sm.sq[tid] = 0.f;
+        if (tid == 0) sm.sp = 0.f;
     } else if (tid < 64) {
-        koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
+        sm.koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
     }
     const T *Xl = g.ptrs ? (const T *)g.ptrs[l] : X + group_offset(g.gl, g.t, l);
     __syncthreads();
     if (g.rows_fast) {  // lanes walk rows: reduce over the warp per k
         const int64_t r = r0 + tx;
         for (int kk = ty; kk < 32; kk += 8) {
-            float v = (r < g.R && k0 + kk < g.K) ? sq_rel(__ldg(Xl + roff[tx] + koff[kk]), be_max) : 0.f;
+            float v = (r < g.R && k0 + kk < g.K) ? sq_rel(__ldg(Xl + sm.roff[tx] + sm.koff[kk]), be_max) : 0.f;
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-            if (tx == 0) atomicAdd(&sq[kk], v);
+            if (tx == 0) atomicAdd(&sm.sq[kk], v);
         }
     } else {  // lanes walk k
         float v = 0.f;
         for (int j = 0; j < 4; ++j) {
             const int rr = ty + 8 * j;
-            if (r0 + rr < g.R && k0 + tx < g.K) v += sq_rel(__ldg(Xl + roff[rr] + koff[tx]), be_max);
+            if (r0 + rr < g.R && k0 + tx < g.K) v += sq_rel(__ldg(Xl + sm.roff[rr] + sm.koff[tx]), be_max);
         }
-        atomicAdd(&sq[tx], v);
+        atomicAdd(&sm.sq[tx], v);
     }
     if (tk == 0 && tid < 32) {
         float w = 0.f;
@@ -409,19 +428,24 @@ __global__ void __launch_bounds__(256) k_oz_stat(const T *__restrict__ X, OpGeom
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) w += __shfl_xor_sync(0xffffffffu, w, d);
-        if (tid == 0) sp = w;
+        if (tid == 0) sm.sp = w;
     }
     __syncthreads();
-    if (tid < 32 && k0 + tid < g.K && sq[tid] != 0.f) atomicAdd(q + l * g.K + k0 + tid, sq[tid]);
-    if (tid == 0 && tk == 0 && sp != 0.f) atomicAdd(P + l, sp);
+    if (tid < 32 && k0 + tid < g.K && sm.sq[tid] != 0.f) atomicAdd(q + l * g.K + k0 + tid, sm.sq[tid]);
+    if (tid == 0 && tk == 0 && sm.sp != 0.f) atomicAdd(P + l, sm.sp);
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_oz_stat(const T *__restrict__ X, OpGeom g, const int32_t *__restrict__ exps,
+                                                 OzStats *st, int t, float *q, float *P) {
+    __shared__ StatSmem sm;
+    oz_stat_tile<T>(X, g, exps, st, t, q, P, blockIdx.x, blockIdx.y, sm);
 }
 
 // One block: the error estimate of every candidate slice count (bit S of
 // `cand`) and the choice, the smallest count within `tol`, else 0 (plain).
-__global__ void __launch_bounds__(1024) k_oz_choose(OzStats *st, const float *__restrict__ qa,
-                                                    const float *__restrict__ qb, const float *__restrict__ pa,
-                                                    const float *__restrict__ pb, int64_t K, int64_t L,
-                                                    uint32_t cand, double tol, double margin, int cx) {
+__device__ __forceinline__ void oz_choose_body(OzStats *st, const float *__restrict__ qa, const float *__restrict__ qb,
+                                               const float *__restrict__ pa, const float *__restrict__ pb, int64_t K,
+                                               int64_t L, uint32_t cand, double tol, double margin, int cx) {
     __shared__ double red[3][32];
     double trunc = 0.0, drop = 0.0, den = 0.0;
     for (int64_t l = 0; l < L; ++l) {
@@ -474,6 +498,12 @@ __global__ void __launch_bounds__(1024) k_oz_choose(OzStats *st, const float *__
     }
     st->est[0] = 0.f;
     st->sel = sel;
+}
+__global__ void __launch_bounds__(1024) k_oz_choose(OzStats *st, const float *__restrict__ qa,
+                                                    const float *__restrict__ qb, const float *__restrict__ pa,
+                                                    const float *__restrict__ pb, int64_t K, int64_t L,
+                                                    uint32_t cand, double tol, double margin, int cx) {
+    oz_choose_body(st, qa, qb, pa, pb, K, L, cand, tol, margin, cx);
 }
 
 // =============================================================================
@@ -558,35 +588,33 @@ struct OzIn<float2> {
 };
 
 // BF3 = true: float inputs split into bf16 pieces; otherwise Ozaki digits.
-// `sel` (nullable): the adaptive choice; the slice count is read from it and
-// the launch does nothing when it is 0 (plain).
+template <typename T, int KT>
+struct SliceSmem {
+    T tile[32][KT + 1];
+    int64_t roff[32], koff[KT];
+    int rexp[32];
+};
+template <typename T, int MODE>
+using SliceSmemOf = SliceSmem<T, MODE == MODE_REAL ? 64 : 32>;
+
 template <typename T, int MODE, bool BF3>
-__global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, OpGeom g,
-                                                  const int32_t *__restrict__ exps, int S, int W,
-                                                  uint32_t *__restrict__ out, int64_t rows_e,
-                                                  int64_t kw, const int32_t *__restrict__ sel) {
-    if (sel) {
-        S = *sel;
-        if (S == 0) return;
-        W = S <= 6 ? 8 : 7;
-    }
+__device__ __forceinline__ void oz_slice_tile(const T *__restrict__ X, const OpGeom &g,
+                                              const int32_t *__restrict__ exps, int S, int W,
+                                              uint32_t *__restrict__ out, int64_t rows_e, int64_t kw, int64_t blk,
+                                              int64_t l, SliceSmemOf<T, MODE> &sm) {
     constexpr int KT = MODE == MODE_REAL ? 64 : 32;  // k per tile
-    __shared__ T tile[32][KT + 1];
-    __shared__ int64_t roff[32], koff[KT];
-    __shared__ int rexp[32];
     int64_t tiles_k = (g.K + KT - 1) / KT;
-    int64_t tr = blockIdx.x / tiles_k, tk = blockIdx.x - tr * tiles_k;
-    int64_t l = blockIdx.y;
+    int64_t tr = blk / tiles_k, tk = blk - tr * tiles_k;
     int64_t r0 = tr * 32, k0 = tk * KT;
     int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
     if (tid < 32) {
-        roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
+        sm.roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
         if (!BF3) {
             int be = (r0 + tid < g.R) ? exps[l * g.R + r0 + tid] : 0;
-            rexp[tid] = be == 0x7FF ? 0x7FFFFFFF : (be == 0 ? -1022 : be - 1022);
+            sm.rexp[tid] = be == 0x7FF ? 0x7FFFFFFF : (be == 0 ? -1022 : be - 1022);
         }
     }
-    if (tid < KT) koff[tid] = (k0 + tid < g.K) ? group_offset(g.gk, g.t, k0 + tid) : 0;
+    if (tid < KT) sm.koff[tid] = (k0 + tid < g.K) ? group_offset(g.gk, g.t, k0 + tid) : 0;
     const T *Xl = g.ptrs ? (const T *)g.ptrs[l] : X + group_offset(g.gl, g.t, l);
     __syncthreads();
     for (int idx = tid; idx < 32 * KT; idx += 256) {
@@ -600,8 +628,8 @@ __global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, Op
         }
         T v;
         memset(&v, 0, sizeof(T));
-        if (r0 + r < g.R && k0 + kk < g.K) v = __ldg(Xl + roff[r] + koff[kk]);
-        tile[r][kk] = v;
+        if (r0 + r < g.R && k0 + kk < g.K) v = __ldg(Xl + sm.roff[r] + sm.koff[kk]);
+        sm.tile[r][kk] = v;
     }
     __syncthreads();
     const int64_t plane = rows_e * kw;
@@ -612,7 +640,7 @@ __global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, Op
         int r = ty + 8 * j;
         int64_t row = r0 + r;
         if (row >= g.R) continue;
-        int e = BF3 ? 0 : rexp[r];
+        int e = BF3 ? 0 : sm.rexp[r];
         bool bad = !BF3 && e == 0x7FFFFFFF;
         if (bad) e = 0;
         if (MODE == MODE_REAL) {
@@ -621,13 +649,13 @@ __global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, Op
             uint32_t *o = outl + row * kw + word;
             if (BF3) {
                 uint32_t p0[8], p1[8];
-                bf3_pieces((float)OzIn<T>::re(tile[r][2 * tx]), p0);
-                bf3_pieces((float)OzIn<T>::re(tile[r][2 * tx + 1]), p1);
+                bf3_pieces((float)OzIn<T>::re(sm.tile[r][2 * tx]), p0);
+                bf3_pieces((float)OzIn<T>::re(sm.tile[r][2 * tx + 1]), p1);
 #pragma unroll
                 for (int s = 0; s < 3; ++s) o[s * plane] = pack2(p0[s], p1[s]);
             } else {
-                int64_t q0 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx]), e);
-                int64_t q1 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(tile[r][2 * tx + 1]), e);
+                int64_t q0 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx]), e);
+                int64_t q1 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx + 1]), e);
 #pragma unroll 1
                 for (int s = 0; s < S; ++s, o += plane) {
                     const int shift = 62 - W * (s + 1);
@@ -642,9 +670,9 @@ __global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, Op
             uint32_t *o = outl + (MODE == MODE_CB ? 2 * row : row) * kw + word;
             if (BF3) {
                 uint32_t pr[8], pi[8], pn[8];
-                bf3_pieces((float)OzIn<T>::re(tile[r][tx]), pr);
-                bf3_pieces((float)OzIn<T>::im(tile[r][tx]), pi);
-                float nim = -(float)OzIn<T>::im(tile[r][tx]);
+                bf3_pieces((float)OzIn<T>::re(sm.tile[r][tx]), pr);
+                bf3_pieces((float)OzIn<T>::im(sm.tile[r][tx]), pi);
+                float nim = -(float)OzIn<T>::im(sm.tile[r][tx]);
                 bf3_pieces(nim, pn);
 #pragma unroll
                 for (int s = 0; s < 3; ++s) {
@@ -656,8 +684,8 @@ __global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, Op
                     }
                 }
             } else {
-                int64_t qr = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(tile[r][tx]), e);
-                int64_t qi = oz_fixed(bad ? 0.0 : (double)OzIn<T>::im(tile[r][tx]), e);
+                int64_t qr = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][tx]), e);
+                int64_t qi = oz_fixed(bad ? 0.0 : (double)OzIn<T>::im(sm.tile[r][tx]), e);
 #pragma unroll 1
                 for (int s = 0; s < S; ++s, o += plane) {
                     const int shift = 62 - W * (s + 1);
@@ -673,6 +701,22 @@ __global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, Op
             }
         }
     }
+}
+
+// `sel` (nullable): the adaptive choice; the slice count is read from it and
+// the launch does nothing when it is 0 (plain).
+template <typename T, int MODE, bool BF3>
+__global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, OpGeom g,
+                                                  const int32_t *__restrict__ exps, int S, int W,
+                                                  uint32_t *__restrict__ out, int64_t rows_e,
+                                                  int64_t kw, const int32_t *__restrict__ sel) {
+    if (sel) {
+        S = *sel;
+        if (S == 0) return;
+        W = S <= 6 ? 8 : 7;
+    }
+    __shared__ SliceSmemOf<T, MODE> sm;
+    oz_slice_tile<T, MODE, BF3>(X, g, exps, S, W, out, rows_e, kw, blockIdx.x, blockIdx.y, sm);
 }
 
 // =============================================================================
@@ -708,6 +752,7 @@ struct OzJob {  // aligned as its tensor maps
 // visits its tiles in increasing order, so the next tile usually lies in the
 // same job or the one after it.
 struct OzOneJob {
+    static constexpr bool kTable = false;
     const OzJob *j;
     __device__ int64_t tiles() const { return (int64_t)j->tiles_n * j->tiles_m * j->L; }
     __device__ const OzJob &job(int64_t t, int64_t &local, int &) const {
@@ -716,6 +761,7 @@ struct OzOneJob {
     }
 };
 struct OzJobTable {
+    static constexpr bool kTable = true;  // jobs may carry their own adaptive choice (skipped unless it is S)
     const OzJob *jobs;
     const int64_t *start;  // [n + 1]: first tile of each job, then the total
     int n;
@@ -837,7 +883,7 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
         const OzGemmArgs &a0 = src.job(0, unused, h0).a;
         // an adaptive plan launches every candidate; all but the chosen one
         // return before touching shared memory or TMEM
-        if (a0.sel && *a0.sel != S) return;
+        if (!Src::kTable && a0.sel && *a0.sel != S) return;
         status = a0.status;
     }
 
@@ -887,6 +933,7 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
             for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
                 int64_t local;
                 const OzJob &J = src.job(t, local, hint);
+                if (Src::kTable && J.a.sel && *J.a.sel != S) continue;  // a job of another slice count
                 int64_t m0, n0;
                 int l;
                 oz_tile(J, local, BN, m0, n0, l);
@@ -923,6 +970,7 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
             for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
                 int64_t local;
                 const OzJob &J = src.job(t, local, hint);
+                if (Src::kTable && J.a.sel && *J.a.sel != S) continue;  // a job of another slice count
                 const int nkb = J.a.nkb, kcb = J.a.kcb;
                 for (int c0 = 0; c0 < nkb && ok; c0 += kcb, ++C) {
                     const uint32_t bank = C & 1u;
@@ -971,6 +1019,7 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
         for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
             int64_t local;
             const OzJob &J = src.job(t, local, hint);
+            if (Src::kTable && J.a.sel && *J.a.sel != S) continue;  // a job of another slice count
             const OzGemmArgs &args = J.a;
             int64_t m0, n0;
             int l;
@@ -1407,6 +1456,19 @@ static int run_stat(const OpGeom &g, const void *X, const int32_t *exps, OzStats
     return MGB_OK;
 }
 
+// Calls f with a null pointer of the operand's element type.
+template <typename F>
+static int by_type(int dtype, F &&f) {
+    switch (dtype) {
+    case MGB_F64: return f((double *)nullptr);
+    case MGB_C64: return f((double2 *)nullptr);
+    case MGB_F32: return f((float *)nullptr);
+    default: return f((float2 *)nullptr);
+    }
+}
+template <typename P>
+using TypeOf = typename std::remove_pointer<P>::type;
+
 // Pre-pass of the emulated forms: exponents (OZAKI) and slices of A and B
 // into the workspace.
 int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *ws, cudaStream_t s) {
@@ -1440,16 +1502,18 @@ int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *
             sel = &sa_.st->sel;
         }
         int32_t *emax_a = p.adaptive ? &sa_.st->emax[0] : nullptr, *emax_b = p.adaptive ? &sa_.st->emax[1] : nullptr;
-        st = p.a.dtype == MGB_C64 ? run_scale<double2>(ga, A, ea, p.L, s, emax_a) : run_scale<double>(ga, A, ea, p.L, s, emax_a);
+        st = by_type(p.a.dtype, [&](auto tag) { return run_scale<TypeOf<decltype(tag)>>(ga, A, ea, p.L, s, emax_a); });
         if (st) return st;
-        st = p.b.dtype == MGB_C64 ? run_scale<double2>(gb, B, eb, p.L, s, emax_b) : run_scale<double>(gb, B, eb, p.L, s, emax_b);
+        st = by_type(p.b.dtype, [&](auto tag) { return run_scale<TypeOf<decltype(tag)>>(gb, B, eb, p.L, s, emax_b); });
         if (st) return st;
         if (p.adaptive) {
-            st = p.a.dtype == MGB_C64 ? run_stat<double2>(ga, A, ea, sa_.st, 0, sa_.qa, sa_.pa, p.L, s)
-                                      : run_stat<double>(ga, A, ea, sa_.st, 0, sa_.qa, sa_.pa, p.L, s);
+            st = by_type(p.a.dtype, [&](auto tag) {
+                return run_stat<TypeOf<decltype(tag)>>(ga, A, ea, sa_.st, 0, sa_.qa, sa_.pa, p.L, s);
+            });
             if (st) return st;
-            st = p.b.dtype == MGB_C64 ? run_stat<double2>(gb, B, eb, sa_.st, 1, sa_.qb, sa_.pb, p.L, s)
-                                      : run_stat<double>(gb, B, eb, sa_.st, 1, sa_.qb, sa_.pb, p.L, s);
+            st = by_type(p.b.dtype, [&](auto tag) {
+                return run_stat<TypeOf<decltype(tag)>>(gb, B, eb, sa_.st, 1, sa_.qb, sa_.pb, p.L, s);
+            });
             if (st) return st;
             // Fluctuations of a Frobenius norm over few outputs: a margin that
             // vanishes for large results.
@@ -1458,11 +1522,13 @@ int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *
                                            margin, cx ? 1 : 0);
             MGB_CUDA_CHECK(cudaGetLastError());
         }
-        st = p.a.dtype == MGB_C64 ? run_prepass<double2, false>(ga, mode_a, A, ea, S, sa, p.m_e, kw, p.L, s, sel)
-                                  : run_prepass<double, false>(ga, mode_a, A, ea, S, sa, p.m_e, kw, p.L, s, sel);
+        st = by_type(p.a.dtype, [&](auto tag) {
+            return run_prepass<TypeOf<decltype(tag)>, false>(ga, mode_a, A, ea, S, sa, p.m_e, kw, p.L, s, sel);
+        });
         if (st) return st;
-        st = p.b.dtype == MGB_C64 ? run_prepass<double2, false>(gb, mode_b, B, eb, S, sb, p.n_e, kw, p.L, s, sel)
-                                  : run_prepass<double, false>(gb, mode_b, B, eb, S, sb, p.n_e, kw, p.L, s, sel);
+        st = by_type(p.b.dtype, [&](auto tag) {
+            return run_prepass<TypeOf<decltype(tag)>, false>(gb, mode_b, B, eb, S, sb, p.n_e, kw, p.L, s, sel);
+        });
         if (st) return st;
     } else {
         st = p.a.dtype == MGB_C32 ? run_prepass<float2, true>(ga, mode_a, A, nullptr, 3, sa, p.m_e, kw, p.L, s)
@@ -1631,4 +1697,365 @@ void ozaki_grouped_destroy(OzGrouped *g) {
     delete g;
 }
 
+
+// =============================================================================
+// Batched execution of many different contractions (the serving form): one
+// launch per pre-pass phase over a table of operands, one multi-job chooser,
+// and one persistent tensor-core launch per kernel variant over a table of
+// (contraction, slice count) jobs.
+// =============================================================================
+enum { PRE_ZERO = 0, PRE_SCALE = 1, PRE_STAT = 2, PRE_SLICE = 3, PRE_PHASES = 4 };
+
+// One operand of one contraction.
+struct PreJob {
+    OpGeom g;
+    const void *X;
+    int32_t dtype;      // the operand's element type
+    int32_t mode;       // MODE_REAL / MODE_CA / MODE_CB
+    int32_t bf3;        // BF16X3 pieces instead of Ozaki digits
+    int32_t S;          // slice count when `sel` is null
+    int32_t t;          // 0 = A, 1 = B
+    int32_t L;
+    int32_t *exps;      // [L][R] (Ozaki)
+    int32_t *emax;      // largest exponent of the operand (adaptive) or null
+    uint32_t *out;      // slice planes
+    int64_t rows_e, kw;
+    const int32_t *sel; // adaptive choice of the contraction, or null
+    OzStats *st;        // its statistics (adaptive) or null
+    float *q, *P;       // this operand's per-k norms and squared scales
+    void *zero[2];      // regions cleared by PRE_ZERO (exponents; statistics for t == 0)
+    int64_t zero_words[2];
+    int64_t tiles[PRE_PHASES];  // blocks of every phase
+};
+
+// One adaptive contraction for the multi-job chooser.
+struct ChooseJob {
+    OzStats *st;
+    const float *qa, *qb, *pa, *pb;
+    int64_t K, L;
+    uint32_t cand;
+    int32_t cx;
+    double tol, margin;
+};
+
+union PreSmem {
+    ScaleSmem scale;
+    StatSmem stat;
+    SliceSmemOf<double, MODE_REAL> s_dr;
+    SliceSmemOf<double2, MODE_CA> s_zc;
+    SliceSmemOf<double, MODE_CA> s_dc;
+    SliceSmemOf<float, MODE_REAL> s_fr;
+    SliceSmemOf<float2, MODE_CA> s_cc;
+    SliceSmemOf<float, MODE_CA> s_fc;
+};
+
+template <typename T, bool BF3>
+__device__ __forceinline__ void pre_slice_typed(const PreJob &J, int S, int W, int64_t blk, int64_t l, PreSmem &sm) {
+    const T *X = (const T *)J.X;
+    switch (J.mode) {
+    case MODE_REAL:
+        if constexpr (!OzIn<T>::cx)
+            oz_slice_tile<T, MODE_REAL, BF3>(X, J.g, J.exps, S, W, J.out, J.rows_e, J.kw, blk, l,
+                                             *reinterpret_cast<SliceSmemOf<T, MODE_REAL> *>(&sm));
+        break;
+    case MODE_CA:
+        oz_slice_tile<T, MODE_CA, BF3>(X, J.g, J.exps, S, W, J.out, J.rows_e, J.kw, blk, l,
+                                       *reinterpret_cast<SliceSmemOf<T, MODE_CA> *>(&sm));
+        break;
+    default:
+        oz_slice_tile<T, MODE_CB, BF3>(X, J.g, J.exps, S, W, J.out, J.rows_e, J.kw, blk, l,
+                                       *reinterpret_cast<SliceSmemOf<T, MODE_CB> *>(&sm));
+        break;
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) k_oz_pre_multi(const PreJob *__restrict__ jobs,
+                                                         const int64_t *__restrict__ start, int njobs, int phase) {
+    __shared__ __align__(16) PreSmem sm;
+    const int64_t b = blockIdx.x;
+    int lo = 0, hi = njobs - 1;  // the last job whose first block is <= b
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (start[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const PreJob &J = jobs[lo];
+    const int64_t local = b - start[lo];
+    if (phase == PRE_ZERO) {
+        for (int r = 0; r < 2; ++r) {  // this job's blocks clear both regions
+            int32_t *z = (int32_t *)J.zero[r];
+            const int64_t n = J.zero_words[r], nb = J.tiles[PRE_ZERO];
+            for (int64_t w = local * blockDim.x + threadIdx.x; w < n; w += nb * blockDim.x) z[w] = 0;
+        }
+        return;
+    }
+    const int64_t per_l = J.tiles[phase] / max(J.L, 1);
+    const int64_t l = local / per_l, blk = local - l * per_l;
+    if (phase == PRE_SCALE) {
+        switch (J.dtype) {
+        case MGB_F64: oz_scale_tile<double>((const double *)J.X, J.g, J.exps, J.emax, blk, l, sm.scale); break;
+        case MGB_C64: oz_scale_tile<double2>((const double2 *)J.X, J.g, J.exps, J.emax, blk, l, sm.scale); break;
+        case MGB_F32: oz_scale_tile<float>((const float *)J.X, J.g, J.exps, J.emax, blk, l, sm.scale); break;
+        default: oz_scale_tile<float2>((const float2 *)J.X, J.g, J.exps, J.emax, blk, l, sm.scale); break;
+        }
+    } else if (phase == PRE_STAT) {
+        switch (J.dtype) {
+        case MGB_F64: oz_stat_tile<double>((const double *)J.X, J.g, J.exps, J.st, J.t, J.q, J.P, blk, l, sm.stat); break;
+        case MGB_C64: oz_stat_tile<double2>((const double2 *)J.X, J.g, J.exps, J.st, J.t, J.q, J.P, blk, l, sm.stat); break;
+        case MGB_F32: oz_stat_tile<float>((const float *)J.X, J.g, J.exps, J.st, J.t, J.q, J.P, blk, l, sm.stat); break;
+        default: oz_stat_tile<float2>((const float2 *)J.X, J.g, J.exps, J.st, J.t, J.q, J.P, blk, l, sm.stat); break;
+        }
+    } else {
+        int S = J.S;
+        if (J.sel) {
+            S = *J.sel;
+            if (S == 0) return;  // the plain form will run this contraction
+        }
+        if (J.bf3) {
+            if (J.dtype == MGB_C32) pre_slice_typed<float2, true>(J, 3, 0, blk, l, sm);
+            else pre_slice_typed<float, true>(J, 3, 0, blk, l, sm);
+        } else {
+            const int W = oz_digit_bits(S);
+            switch (J.dtype) {
+            case MGB_F64: pre_slice_typed<double, false>(J, S, W, blk, l, sm); break;
+            case MGB_C64: pre_slice_typed<double2, false>(J, S, W, blk, l, sm); break;
+            case MGB_F32: pre_slice_typed<float, false>(J, S, W, blk, l, sm); break;
+            default: pre_slice_typed<float2, false>(J, S, W, blk, l, sm); break;
+            }
+        }
+    }
+}
+
+// dst[i] = *src[i]: every item's slice count after the choice
+__global__ void k_gather_sel(const int32_t *const *__restrict__ src, int32_t *__restrict__ dst, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = *src[i];
+}
+
+// One block per adaptive contraction (the body of k_oz_choose).
+__global__ void __launch_bounds__(1024) k_oz_choose_multi(const ChooseJob *__restrict__ jobs) {
+    const ChooseJob &c = jobs[blockIdx.x];
+    oz_choose_body(c.st, c.qa, c.qb, c.pa, c.pb, c.K, c.L, c.cand, c.tol, c.margin, c.cx);
+}
+
+struct OzBatchBuffers {
+    // device tables and their pinned staging, grown on demand
+    uint8_t *dev = nullptr, *host = nullptr;
+    size_t cap = 0;
+    cudaEvent_t staged = nullptr;  // the last upload has left the staging area
+};
+
+OzBatchBuffers *ozaki_batch_buffers_create() { return new OzBatchBuffers(); }
+
+void ozaki_batch_buffers_destroy(OzBatchBuffers *b) {
+    if (!b) return;
+    if (b->staged) cudaEventSynchronize(b->staged), cudaEventDestroy(b->staged);
+    if (b->dev) cudaFree(b->dev);
+    if (b->host) cudaFreeHost(b->host);
+    delete b;
+}
+
+static int batch_reserve(OzBatchBuffers *b, size_t bytes) {
+    if (b->staged) MGB_CUDA_CHECK(cudaEventSynchronize(b->staged));  // the previous upload read the staging
+    if (bytes <= b->cap) return MGB_OK;
+    size_t cap = std::max(bytes, 2 * b->cap);
+    if (b->dev) cudaFree(b->dev);
+    if (b->host) cudaFreeHost(b->host);
+    b->dev = b->host = nullptr;
+    b->cap = 0;
+    MGB_CUDA_CHECK(cudaMalloc((void **)&b->dev, cap));
+    MGB_CUDA_CHECK(cudaMallocHost((void **)&b->host, cap));
+    b->cap = cap;
+    if (!b->staged) MGB_CUDA_CHECK(cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming));
+    return MGB_OK;
+}
+
+static void fill_prejob(PreJob &J, const ContractionPlan &p, int t, const void *X, void *ws) {
+    std::memset(&J, 0, sizeof(J));
+    const bool cx = is_complex(p.compute_dtype), exact = p.form == MGB_FORM_OZAKI;
+    uint8_t *w = (uint8_t *)ws;
+    J.g.ptrs = nullptr;
+    J.g.gr = t == 0 ? p.gm : p.gn;
+    J.g.gk = p.gk;
+    J.g.gl = p.gl;
+    J.g.t = t;
+    J.g.R = t == 0 ? p.M : p.N;
+    J.g.K = p.K;
+    J.g.rows_fast = unit_row_fast(J.g.gr, p.gk, t);
+    J.X = X;
+    J.dtype = t == 0 ? p.a.dtype : p.b.dtype;
+    J.mode = cx ? (t == 0 ? MODE_CA : MODE_CB) : MODE_REAL;
+    J.bf3 = exact ? 0 : 1;
+    J.S = exact ? p.slices : 3;
+    J.t = t;
+    J.L = (int32_t)p.L;
+    J.exps = exact ? (int32_t *)(w + (t == 0 ? p.ws_scale_a : p.ws_scale_b)) : nullptr;
+    J.out = (uint32_t *)(w + (t == 0 ? p.ws_a : p.ws_b));
+    J.rows_e = t == 0 ? p.m_e : p.n_e;
+    J.kw = p.kpad / 2;
+    const int64_t R = J.g.R, K = p.K, L = p.L;
+    const int KT = J.mode == MODE_REAL ? 64 : 32;
+    int64_t zw = 0;
+    if (exact) {
+        J.zero[0] = J.exps;
+        J.zero_words[0] = L * R;
+        zw += L * R;
+        if (p.adaptive) {
+            OzStatArea a = stat_area(p, ws);
+            J.sel = &a.st->sel;
+            J.st = a.st;
+            J.emax = &a.st->emax[t];
+            J.q = t == 0 ? a.qa : a.qb;
+            J.P = t == 0 ? a.pa : a.pb;
+            if (t == 0) {
+                J.zero[1] = a.st;
+                J.zero_words[1] = (int64_t)(stat_bytes(p) / 4);
+                zw += J.zero_words[1];
+            }
+        }
+    }
+    J.tiles[PRE_ZERO] = zw ? std::min<int64_t>((zw + 1023) / 1024, 64) : 0;
+    const int64_t tiles32 = ((R + 31) / 32) * ((K + 31) / 32) * L;
+    J.tiles[PRE_SCALE] = exact ? tiles32 : 0;
+    J.tiles[PRE_STAT] = (exact && p.adaptive) ? tiles32 : 0;
+    J.tiles[PRE_SLICE] = ((R + 31) / 32) * ((K + KT - 1) / KT) * L;
+}
+
+int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *buf, cudaStream_t s,
+                       int32_t *sel_dev_out, const std::function<int()> &after_prepass,
+                       const std::function<int(int S, bool exact, bool cx)> &after_variant) {
+    const int n = (int)items.size();
+    if (n == 0) return MGB_OK;
+    int32_t *status = device_status_ptr();
+    if (!status) return fail(MGB_ERR_CUDA, "device status word unavailable");
+    // ---- host tables
+    std::vector<PreJob> pre(2 * n);
+    std::vector<ChooseJob> choose;
+    // GEMM jobs per variant: key (S, exact, cx) ordered cheapest first
+    std::map<std::tuple<int, int, int>, std::vector<OzJob>> gem;
+    for (int i = 0; i < n; ++i) {
+        const OzBatchItem &it = items[i];
+        const ContractionPlan &p = *it.p;
+        if (p.form == MGB_FORM_PLAIN) return fail(MGB_ERR_ARGUMENT, "batch: plain-form plans are not batched");
+        if (((uintptr_t)it.ws & 255) != 0) return fail(MGB_ERR_WORKSPACE, "batch: workspace must be 256-byte aligned");
+        fill_prejob(pre[2 * i], p, 0, it.A, it.ws);
+        fill_prejob(pre[2 * i + 1], p, 1, it.B, it.ws);
+        const bool exact = p.form == MGB_FORM_OZAKI, cx = is_complex(p.compute_dtype);
+        if (p.adaptive) {
+            OzStatArea a = stat_area(p, it.ws);
+            ChooseJob c;
+            c.st = a.st;
+            c.qa = a.qa;
+            c.qb = a.qb;
+            c.pa = a.pa;
+            c.pb = a.pb;
+            c.K = p.K;
+            c.L = p.L;
+            c.cand = p.cand_mask;
+            c.cx = cx ? 1 : 0;
+            c.tol = p.tol;
+            c.margin = 1.0 + 2.0 / std::sqrt((double)std::max<int64_t>(p.M * p.N * p.L, 1));
+            choose.push_back(c);
+            for (int S = 3; S <= 8; ++S) {
+                if (!(p.cand_mask & (1u << S))) continue;
+                OzJob job;
+                int64_t tiles;
+                if (int st = ozaki_job(p, it.C, it.ws, job, tiles, S, &a.st->sel)) return st;
+                gem[std::make_tuple(S, 1, cx ? 1 : 0)].push_back(job);
+            }
+        } else {
+            OzJob job;
+            int64_t tiles;
+            if (int st = ozaki_job(p, it.C, it.ws, job, tiles)) return st;
+            gem[std::make_tuple(exact ? p.slices : 3, exact ? 1 : 0, cx ? 1 : 0)].push_back(job);
+        }
+    }
+    // ---- one staging area: [pre jobs][pre starts x 4 phases][choose jobs][per variant: jobs, starts][sel]
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    size_t off = 0;
+    const size_t o_pre = off;
+    off = al(off + pre.size() * sizeof(PreJob));
+    const size_t o_pst = off;
+    off = al(off + PRE_PHASES * (pre.size() + 1) * sizeof(int64_t));
+    const size_t o_ch = off;
+    off = al(off + choose.size() * sizeof(ChooseJob));
+    // per item: the address of its slice count (adaptive: the choice; else
+    // the fixed count stored here)
+    const size_t o_fix = off;
+    off = al(off + n * sizeof(int32_t));
+    const size_t o_sp = off;
+    off = al(off + n * sizeof(void *));
+    std::vector<size_t> o_gj, o_gs;
+    for (auto &kv : gem) {
+        o_gj.push_back(off);
+        off = al(off + kv.second.size() * sizeof(OzJob));
+        o_gs.push_back(off);
+        off = al(off + (kv.second.size() + 1) * sizeof(int64_t));
+    }
+    if (int st = batch_reserve(buf, off)) return st;
+    uint8_t *h = buf->host, *d = buf->dev;
+    std::memcpy(h + o_pre, pre.data(), pre.size() * sizeof(PreJob));
+    int64_t *pst = (int64_t *)(h + o_pst);
+    int64_t blocks[PRE_PHASES];
+    for (int ph = 0; ph < PRE_PHASES; ++ph) {
+        int64_t *st = pst + ph * (pre.size() + 1);
+        st[0] = 0;
+        for (size_t j = 0; j < pre.size(); ++j) st[j + 1] = st[j] + pre[j].tiles[ph];
+        blocks[ph] = st[pre.size()];
+    }
+    std::memcpy(h + o_ch, choose.data(), choose.size() * sizeof(ChooseJob));
+    for (int i = 0; i < n; ++i) {
+        const ContractionPlan &p = *items[i].p;
+        ((int32_t *)(h + o_fix))[i] = p.form == MGB_FORM_OZAKI ? p.slices : 3;
+        ((const int32_t **)(h + o_sp))[i] =
+            p.adaptive ? &stat_area(p, items[i].ws).st->sel : (const int32_t *)(d + o_fix) + i;
+    }
+    size_t vi = 0;
+    std::vector<int64_t> vtiles;
+    for (auto &kv : gem) {
+        std::memcpy(h + o_gj[vi], kv.second.data(), kv.second.size() * sizeof(OzJob));
+        int64_t *st = (int64_t *)(h + o_gs[vi]);
+        st[0] = 0;
+        for (size_t j = 0; j < kv.second.size(); ++j)
+            st[j + 1] = st[j] + (int64_t)kv.second[j].tiles_n * kv.second[j].tiles_m * kv.second[j].L;
+        vtiles.push_back(st[kv.second.size()]);
+        ++vi;
+    }
+    MGB_CUDA_CHECK(cudaMemcpyAsync(d, h, off, cudaMemcpyHostToDevice, s));
+    MGB_CUDA_CHECK(cudaEventRecord(buf->staged, s));
+    // ---- pre-pass phases
+    const PreJob *dpre = (const PreJob *)(d + o_pre);
+    for (int ph = 0; ph < PRE_PHASES; ++ph) {
+        if (ph == PRE_SLICE && !choose.empty()) {
+            k_oz_choose_multi<<<(unsigned)choose.size(), 1024, 0, s>>>((const ChooseJob *)(d + o_ch));
+            MGB_CUDA_CHECK(cudaGetLastError());
+        }
+        if (blocks[ph] == 0) continue;
+        if (blocks[ph] > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "batch: pre-pass grid too large");
+        k_oz_pre_multi<<<(unsigned)blocks[ph], 256, 0, s>>>(dpre, (const int64_t *)(d + o_pst) + ph * (pre.size() + 1),
+                                                            (int)pre.size(), ph);
+        MGB_CUDA_CHECK(cudaGetLastError());
+    }
+    // every item's slice count (its fixed count, or the device's choice; 0 = plain)
+    if (sel_dev_out) {
+        k_gather_sel<<<(n + 255) / 256, 256, 0, s>>>((const int32_t *const *)(d + o_sp), sel_dev_out, n);
+        MGB_CUDA_CHECK(cudaGetLastError());
+    }
+    if (after_prepass)
+        if (int st = after_prepass()) return st;
+    // ---- one persistent launch per kernel variant
+    vi = 0;
+    for (auto &kv : gem) {
+        const int S = std::get<0>(kv.first);
+        const bool exact = std::get<1>(kv.first) != 0, cx = std::get<2>(kv.first) != 0;
+        if (vtiles[vi] > 0)
+            if (int st = launch_grouped(S, exact, cx, (const OzJob *)(d + o_gj[vi]), (const int64_t *)(d + o_gs[vi]),
+                                        (int)kv.second.size(), vtiles[vi], s))
+                return st;
+        if (after_variant)
+            if (int st = after_variant(S, exact, cx)) return st;
+        ++vi;
+    }
+    return MGB_OK;
+}
 }  // namespace mgb

@@ -1,28 +1,40 @@
 // Serving loop: contractions submitted as they arrive, admitted against a
-// device-memory byte budget, and dispatched with continuous batching onto
-// several streams so that requests arriving while others run overlap with
-// them on the GPU.
+// device-memory byte budget, and run as batched launches with continuous
+// batching over several streams, so that requests arriving while others run
+// join the next batch and overlap with the running ones on the GPU.
 //
 // A scheduler thread owned by the server repeatedly
-//   1. retires finished batches (event query), releasing their budget and
-//      waking the waiters of their requests;
+//   1. retires finished requests one by one: every request waits on the event
+//      of the launch that computed it, not on the whole batch;
 //   2. admits queued requests in arrival order while the bytes of admitted,
 //      unfinished requests (operands, output and workspace) stay within the
-//      budget, and launches them as one batch on an idle stream: every
-//      request's workspace comes from the server's stream-ordered memory pool
-//      (cudaMallocAsync / cudaFreeAsync, no device synchronisation);
-//   3. sleeps briefly when there is nothing to do.
-// Latency is measured from submission to the moment the scheduler sees the
-// request's batch finished. Plans and device buffers stay owned by the caller,
-// who must keep them alive until the request is finished.
+//      budget, and launches them as one batch on an idle stream:
+//        - the emulated-form requests (Ozaki, BF16x3; each with its own
+//          shapes) through the batched path: one launch per pre-pass phase
+//          over all of their operands, the adaptive slice choices in one
+//          launch, and one persistent tensor-core launch per kernel variant,
+//          each followed by an event that retires the requests it computed;
+//        - plain-form requests one launch each, each with its own event;
+//      a batch takes one workspace block from the server's stream-ordered
+//      memory pool (cudaMallocFromPoolAsync, no device synchronisation);
+//   3. re-runs through mgb_contract the adaptive requests whose device
+//      choice was the plain form (their estimate met no slice count);
+//   4. sleeps briefly when there is nothing to do.
+// A request finishes with MGB_ERR_DEVICE_TIMEOUT when the device status word
+// (bounded waits of the kernels) is set at its retirement. Latency is measured
+// from submission to the moment the scheduler sees the request finished.
+// Plans and device buffers stay owned by the caller, who must keep them alive
+// until the request is finished.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <thread>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -40,11 +52,29 @@ struct Req {
     uint64_t bytes;      // admitted bytes: caller-declared resident bytes + workspace
     cudaEvent_t dep;     // caller-stream event the request waits on (or null)
     Clock::time_point t0;
+    cudaEvent_t done = nullptr;    // the launch that computes it (set once known)
+    bool own_done = false;         // `done` belongs to this request alone
+    const int32_t *status_word = nullptr;  // pinned snapshot of the device status after its launch
+    int32_t status = MGB_OK;
 };
 
+// A kernel variant of the batched tensor-core launches: slice count, exact
+// (Ozaki) or not (BF16x3), complex or real.
+typedef std::tuple<int, int, int> Variant;
+constexpr int kMaxVariants = 16;
+
 struct Batch {
-    std::vector<Req> reqs;
-    cudaEvent_t done = nullptr;
+    std::vector<Req> emu;        // emulated-form requests (batched path)
+    std::vector<Req> plain;      // plain-form requests (own launches)
+    std::map<Variant, std::pair<cudaEvent_t, int32_t *>> variant;  // event and status snapshot after its launch
+    cudaEvent_t chosen = nullptr;  // the slice counts have reached sel_host
+    bool mapped = false;           // every emulated request knows its launch
+    void *ws = nullptr;
+    int32_t *sel_dev = nullptr, *sel_host = nullptr;  // per emulated request
+    size_t sel_cap = 0;
+    int32_t *status_host = nullptr;  // pinned: [0] after the plain launches, [1 + v] after variant v
+    cudaEvent_t end = nullptr;       // after everything of the batch
+    mgb::OzBatchBuffers *buf = nullptr;
     bool busy = false;
 };
 
@@ -61,27 +91,36 @@ struct mgb_server_s {
     std::unordered_map<int64_t, int32_t> finished;  // ticket -> status
     std::vector<double> latency_ms;
     std::vector<cudaEvent_t> event_pool;
-    std::mutex mu;
+    std::mutex mu;     // queue, results, statistics and budget
+    std::mutex ev_mu;  // event pool (never held while taking mu)
     std::condition_variable cv_work, cv_done;
     std::atomic<bool> stop{false};
     std::thread worker;
     int64_t next_ticket = 1;
     uint64_t submitted = 0, completed = 0, rejected = 0, batches = 0;
-    double busy_ms = 0;
     Clock::time_point started;
 };
 
 using namespace mgb;
 
 static cudaEvent_t take_event(mgb_server_s *s) {
-    if (!s->event_pool.empty()) {
-        cudaEvent_t e = s->event_pool.back();
-        s->event_pool.pop_back();
-        return e;
+    {
+        std::lock_guard<std::mutex> lk(s->ev_mu);
+        if (!s->event_pool.empty()) {
+            cudaEvent_t e = s->event_pool.back();
+            s->event_pool.pop_back();
+            return e;
+        }
     }
     cudaEvent_t e = nullptr;
     cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     return e;
+}
+
+static void give_event(mgb_server_s *s, cudaEvent_t e) {
+    if (!e) return;
+    std::lock_guard<std::mutex> lk(s->ev_mu);
+    s->event_pool.push_back(e);
 }
 
 static void finish(mgb_server_s *s, const Req &r, int32_t status) {
@@ -90,76 +129,217 @@ static void finish(mgb_server_s *s, const Req &r, int32_t status) {
     s->latency_ms.push_back(std::chrono::duration<double, std::milli>(Clock::now() - r.t0).count());
     s->used -= r.bytes;
     ++s->completed;
-    if (r.dep) s->event_pool.push_back(r.dep);
+    give_event(s, r.dep);
+}
+
+static int alloc_ws(mgb_server_s *s, void **p, uint64_t bytes, cudaStream_t st) {
+    *p = nullptr;
+    if (!bytes) return MGB_OK;
+    return cudaMallocFromPoolAsync(p, bytes, s->pool, st) == cudaSuccess ? MGB_OK : MGB_ERR_OUT_OF_MEMORY;
+}
+
+static Variant variant_of(const ContractionPlan &cp, int S) {
+    return Variant(S, cp.form == MGB_FORM_OZAKI ? 1 : 0, is_complex(cp.compute_dtype) ? 1 : 0);
+}
+
+// Launches the emulated requests of slot k's batch; returns an mgb_status.
+static int launch_emulated(mgb_server_s *s, size_t k) {
+    Batch &b = s->slots[k];
+    cudaStream_t st = s->streams[k];
+    std::vector<uint64_t> off(b.emu.size());
+    uint64_t total = 0;
+    for (size_t i = 0; i < b.emu.size(); ++i) {
+        off[i] = total;
+        total += (b.emu[i].plan->cp.ws_bytes + 255) & ~uint64_t(255);
+    }
+    if (b.sel_cap < b.emu.size()) {
+        if (b.sel_dev) cudaFree(b.sel_dev);
+        if (b.sel_host) cudaFreeHost(b.sel_host);
+        b.sel_dev = b.sel_host = nullptr;
+        b.sel_cap = 0;
+        const size_t cap = std::max<size_t>(b.emu.size(), 64);
+        MGB_CUDA_CHECK(cudaMalloc((void **)&b.sel_dev, cap * 4));
+        MGB_CUDA_CHECK(cudaMallocHost((void **)&b.sel_host, cap * 4));
+        b.sel_cap = cap;
+    }
+    int rc = alloc_ws(s, &b.ws, total, st);
+    if (rc) return rc;
+    std::vector<OzBatchItem> items(b.emu.size());
+    for (size_t i = 0; i < b.emu.size(); ++i)
+        items[i] = {&b.emu[i].plan->cp, b.emu[i].A, b.emu[i].B, b.emu[i].C, (char *)b.ws + off[i]};
+    int nv = 0;
+    rc = ozaki_batch_launch(
+        items, b.buf, st, b.sel_dev,
+        [&]() -> int {  // the slice counts reach the host before any tensor-core launch
+            MGB_CUDA_CHECK(cudaMemcpyAsync(b.sel_host, b.sel_dev, b.emu.size() * 4, cudaMemcpyDeviceToHost, st));
+            b.chosen = take_event(s);
+            MGB_CUDA_CHECK(cudaEventRecord(b.chosen, st));
+            return MGB_OK;
+        },
+        [&](int S, bool exact, bool cx) -> int {
+            if (nv >= kMaxVariants) return fail(MGB_ERR_UNSUPPORTED, "server: too many kernel variants in a batch");
+            int32_t *snap = b.status_host + 1 + nv++;
+            MGB_CUDA_CHECK(cudaMemcpyAsync(snap, device_status_ptr(), 4, cudaMemcpyDeviceToHost, st));
+            cudaEvent_t e = take_event(s);
+            MGB_CUDA_CHECK(cudaEventRecord(e, st));
+            b.variant[Variant(S, exact ? 1 : 0, cx ? 1 : 0)] = {e, snap};
+            return MGB_OK;
+        });
+    cudaFreeAsync(b.ws, st);  // stream-ordered: reusable once the batch has passed this point
+    b.ws = nullptr;
+    return rc;
+}
+
+// Launches one admitted batch on stream k. Requests that fail to launch are
+// finished at once with their error.
+static void launch_batch(mgb_server_s *s, size_t k, std::vector<Req> &reqs) {
+    Batch &b = s->slots[k];
+    cudaStream_t st = s->streams[k];
+    for (auto &r : reqs)
+        if (r.dep) cudaStreamWaitEvent(st, r.dep, 0);
+    std::vector<Req> failed;
+    for (auto &r : reqs) (r.plan->cp.form == MGB_FORM_PLAIN ? b.plain : b.emu).push_back(r);
+    if (!b.emu.empty()) {
+        if (int rc = launch_emulated(s, k)) {
+            for (auto &r : b.emu) {
+                r.status = rc;
+                failed.push_back(r);
+            }
+            b.emu.clear();
+            for (auto &kv : b.variant) give_event(s, kv.second.first);
+            b.variant.clear();
+            give_event(s, b.chosen);
+            b.chosen = nullptr;
+        }
+    }
+    std::vector<Req> ok;
+    for (auto &r : b.plain) {
+        // the plain form reads its operands in place and needs no workspace
+        if (int rc = mgb_contract(r.plan, r.A, r.B, r.C, nullptr, 0, st)) {
+            r.status = rc;
+            failed.push_back(r);
+            continue;
+        }
+        r.done = take_event(s);
+        r.own_done = true;
+        r.status_word = b.status_host;  // plain kernels have no bounded waits; the snapshot is taken below
+        cudaEventRecord(r.done, st);
+        ok.push_back(r);
+    }
+    b.plain.swap(ok);
+    cudaMemcpyAsync(b.status_host, device_status_ptr(), 4, cudaMemcpyDeviceToHost, st);
+    cudaEventRecord(b.end, st);
+    b.mapped = b.emu.empty();
+    b.busy = true;
+    ++s->batches;
+    if (!failed.empty()) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto &r : failed) finish(s, r, r.status);
+        s->cv_done.notify_all();
+    }
+}
+
+// Retires what finished in slot k; returns true when something changed.
+static bool retire(mgb_server_s *s, size_t k) {
+    Batch &b = s->slots[k];
+    if (!b.busy) return false;
+    bool progressed = false;
+    cudaStream_t st = s->streams[k];
+    if (!b.mapped && cudaEventQuery(b.chosen) != cudaErrorNotReady) {
+        // every emulated request now knows the launch that computes it;
+        // adaptive ones that chose the plain form run again through mgb_contract
+        bool redo = false;
+        for (size_t i = 0; i < b.emu.size(); ++i) {
+            Req &r = b.emu[i];
+            const int S = b.sel_host[i];
+            auto it = S > 0 ? b.variant.find(variant_of(r.plan->cp, S)) : b.variant.end();
+            if (it != b.variant.end()) {
+                r.done = it->second.first;
+                r.status_word = it->second.second;
+                continue;
+            }
+            void *ws = nullptr;
+            int rc = alloc_ws(s, &ws, r.plan->cp.ws_bytes, st);
+            if (rc == MGB_OK) rc = mgb_contract(r.plan, r.A, r.B, r.C, ws, r.plan->cp.ws_bytes, st);
+            if (ws) cudaFreeAsync(ws, st);
+            r.status = rc;
+            r.done = take_event(s);
+            r.own_done = true;
+            r.status_word = b.status_host;
+            cudaEventRecord(r.done, st);
+            redo = true;
+        }
+        if (redo) {  // the batch now ends after the re-runs
+            cudaMemcpyAsync(b.status_host, device_status_ptr(), 4, cudaMemcpyDeviceToHost, st);
+            cudaEventRecord(b.end, st);
+        }
+        b.mapped = true;
+        progressed = true;
+    }
+    // one by one: requests whose own launch has completed
+    std::vector<std::pair<Req, int32_t>> done;
+    auto sweep = [&](std::vector<Req> &v) {
+        std::vector<Req> keep;
+        for (auto &r : v) {
+            cudaError_t q = r.done ? cudaEventQuery(r.done) : cudaErrorNotReady;
+            // own events of plain launches and re-runs: their status snapshot
+            // is taken at the batch's end
+            if (q == cudaSuccess && r.own_done && cudaEventQuery(b.end) == cudaErrorNotReady) q = cudaErrorNotReady;
+            if (q == cudaErrorNotReady) {
+                keep.push_back(r);
+                continue;
+            }
+            int32_t stv = r.status;
+            if (stv == MGB_OK && q != cudaSuccess) stv = MGB_ERR_CUDA;
+            // a bounded device wait gave up on this device since the word was
+            // last cleared: the result of this request is suspect
+            if (stv == MGB_OK && r.status_word && *r.status_word != 0) stv = MGB_ERR_DEVICE_TIMEOUT;
+            done.push_back({r, stv});
+            if (r.own_done) give_event(s, r.done);
+        }
+        v.swap(keep);
+    };
+    if (b.mapped) sweep(b.emu);
+    sweep(b.plain);
+    const bool all = b.mapped && b.emu.empty() && b.plain.empty() && cudaEventQuery(b.end) != cudaErrorNotReady;
+    if (all) {
+        for (auto &kv : b.variant) give_event(s, kv.second.first);
+        b.variant.clear();
+        give_event(s, b.chosen);
+        b.chosen = nullptr;
+        b.busy = false;
+        progressed = true;
+    }
+    if (!done.empty()) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto &x : done) finish(s, x.first, x.second);
+        s->cv_done.notify_all();
+        progressed = true;
+    }
+    return progressed;
 }
 
 static void serve_loop(mgb_server_s *s) {
     cudaSetDevice(s->device);
     while (!s->stop.load()) {
         bool progressed = false;
-        // 1. retire finished batches
+        for (size_t k = 0; k < s->slots.size(); ++k) progressed |= retire(s, k);
         for (size_t k = 0; k < s->slots.size(); ++k) {
-            Batch &b = s->slots[k];
-            if (!b.busy) continue;
-            cudaError_t q = cudaEventQuery(b.done);
-            if (q == cudaErrorNotReady) continue;
-            std::lock_guard<std::mutex> lk(s->mu);
-            for (auto &r : b.reqs) finish(s, r, q == cudaSuccess ? MGB_OK : MGB_ERR_CUDA);
-            b.reqs.clear();
-            b.busy = false;
-            progressed = true;
-            s->cv_done.notify_all();
-        }
-        // 2. admit and launch on idle streams
-        for (size_t k = 0; k < s->slots.size(); ++k) {
-            Batch &b = s->slots[k];
-            if (b.busy) continue;
+            if (s->slots[k].busy) continue;
+            std::vector<Req> reqs;
             {
                 std::lock_guard<std::mutex> lk(s->mu);
-                while (!s->pending.empty() && (int)b.reqs.size() < s->max_batch) {
+                while (!s->pending.empty() && (int)reqs.size() < s->max_batch) {
                     Req &r = s->pending.front();
                     if (s->used + r.bytes > s->budget) break;  // wait for budget (FIFO)
                     s->used += r.bytes;
-                    b.reqs.push_back(r);
+                    reqs.push_back(r);
                     s->pending.pop_front();
                 }
             }
-            if (b.reqs.empty()) break;
-            cudaStream_t st = s->streams[k];
-            std::vector<std::pair<size_t, int32_t>> failed;
-            for (size_t i = 0; i < b.reqs.size(); ++i) {
-                Req &r = b.reqs[i];
-                if (r.dep) cudaStreamWaitEvent(st, r.dep, 0);
-                void *ws = nullptr;
-                const uint64_t wsb = r.plan->cp.ws_bytes;
-                if (wsb && cudaMallocFromPoolAsync(&ws, wsb, s->pool, st) != cudaSuccess) {
-                    failed.push_back({i, MGB_ERR_OUT_OF_MEMORY});
-                    continue;
-                }
-                int rc = mgb_contract(r.plan, r.A, r.B, r.C, ws, wsb, st);
-                if (ws) cudaFreeAsync(ws, st);
-                if (rc) failed.push_back({i, rc});
-            }
-            cudaEventRecord(b.done, st);
-            b.busy = true;
-            ++s->batches;
+            if (reqs.empty()) break;
+            launch_batch(s, k, reqs);
             progressed = true;
-            if (!failed.empty()) {
-                // finished (with an error) right away; the rest completes with the batch
-                std::lock_guard<std::mutex> lk(s->mu);
-                std::vector<Req> keep;
-                size_t fi = 0;
-                for (size_t i = 0; i < b.reqs.size(); ++i) {
-                    if (fi < failed.size() && failed[fi].first == i) {
-                        finish(s, b.reqs[i], failed[fi].second);
-                        ++fi;
-                    } else {
-                        keep.push_back(b.reqs[i]);
-                    }
-                }
-                b.reqs.swap(keep);
-                s->cv_done.notify_all();
-            }
         }
         if (!progressed) {
             std::unique_lock<std::mutex> lk(s->mu);
@@ -182,6 +362,10 @@ int mgb_server_create(mgb_server *server, uint64_t budget_bytes, int32_t nstream
         delete s;
         return cuda_fail(e, "cudaGetDevice");
     }
+    if (!device_status_ptr()) {
+        delete s;
+        return fail(MGB_ERR_CUDA, "device status word unavailable");
+    }
     cudaMemPoolProps props;
     std::memset(&props, 0, sizeof(props));
     props.allocType = cudaMemAllocationTypePinned;
@@ -197,7 +381,11 @@ int mgb_server_create(mgb_server *server, uint64_t budget_bytes, int32_t nstream
     s->slots.resize(nstreams);
     for (int i = 0; i < nstreams; ++i) {
         cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking);
-        cudaEventCreateWithFlags(&s->slots[i].done, cudaEventDisableTiming);
+        Batch &b = s->slots[i];
+        cudaEventCreateWithFlags(&b.end, cudaEventDisableTiming);
+        b.buf = ozaki_batch_buffers_create();
+        if (cudaMallocHost((void **)&b.status_host, (1 + kMaxVariants) * 4) == cudaSuccess)
+            std::memset(b.status_host, 0, (1 + kMaxVariants) * 4);
     }
     s->started = Clock::now();
     s->worker = std::thread(serve_loop, s);
@@ -296,7 +484,14 @@ int mgb_server_destroy(mgb_server server) {
     for (size_t i = 0; i < server->streams.size(); ++i) {
         cudaStreamSynchronize(server->streams[i]);
         cudaStreamDestroy(server->streams[i]);
-        cudaEventDestroy(server->slots[i].done);
+        Batch &b = server->slots[i];
+        cudaEventDestroy(b.end);
+        for (auto &kv : b.variant) cudaEventDestroy(kv.second.first);
+        if (b.chosen) cudaEventDestroy(b.chosen);
+        ozaki_batch_buffers_destroy(b.buf);
+        if (b.sel_dev) cudaFree(b.sel_dev);
+        if (b.sel_host) cudaFreeHost(b.sel_host);
+        if (b.status_host) cudaFreeHost(b.status_host);
     }
     for (auto e : server->event_pool) cudaEventDestroy(e);
     if (server->pool) cudaMemPoolDestroy(server->pool);

@@ -88,3 +88,43 @@ def test_concurrent_clients():
     for (A, B, ic, a, b), C in zip(reqs, results):
         tol = 1e-5 if C.dtype == torch.complex64 else 1e-13
         assert ref.rel_fro(C.data.cpu().numpy(), ref.contract(a, [i.tag for i in A.inds], b, [i.tag for i in B.inds], ic)) <= tol
+
+
+def test_one_batch_with_every_kind_of_request():
+    """One batch of Gaussian ComplexF64 requests, Float64 requests with a
+    dominant column (more slices), Float64 requests whose inversely scaled
+    columns and rows defeat row scaling (the device chooses the plain form and
+    the server runs them again), and ComplexF32 requests (BF16x3): every
+    result equals the same contraction run alone and meets the oracle."""
+    import muscle_gb300 as m
+
+    rng = np.random.default_rng(21)
+    arrays = []
+    for kind in ["gauss"] * 6 + ["dominant"] * 2 + ["kscaled"] * 2 + ["c32"] * 3:
+        M, K, N = (int(x) for x in rng.integers(40, 300, size=3))
+        if kind in ("gauss", "c32"):
+            dt = np.complex128 if kind == "gauss" else np.complex64
+            a = (rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))).astype(dt)
+            b = (rng.standard_normal((K, N)) + 1j * rng.standard_normal((K, N))).astype(dt)
+        else:
+            a, b = rng.standard_normal((M, K)), rng.standard_normal((K, N))
+            if kind == "dominant":
+                a[:, 1] *= 1e6
+            else:
+                s = np.exp2(rng.uniform(-20, 20, K))
+                a, b = a * s[None, :], b / s[:, None]
+        arrays.append((np.asfortranarray(a), np.asfortranarray(b), kind))
+    tens = [(m.Tensor(torch.from_numpy(a).cuda(), ["i", "k"]), m.Tensor(torch.from_numpy(b).cuda(), ["k", "j"]))
+            for a, b, _ in arrays]
+    torch.cuda.synchronize()
+    with m.Server(budget_bytes=4 << 30, streams=2, max_batch=64, form="auto") as srv:
+        pending = [srv.submit(A, B, out=["i", "j"]) for A, B in tens]
+        outs = [p.result(timeout=120) for p in pending]
+        st = srv.stats()
+    assert st["completed"] == len(arrays) and st["rejected"] == 0
+    for (a, b, kind), (A, B), C in zip(arrays, tens, outs):
+        got = C.data.cpu().numpy()
+        alone = m.binary_einsum(A, B, out=["i", "j"]).data.cpu().numpy()
+        assert np.array_equal(got, alone), kind
+        tol = 1e-5 if kind == "c32" else 1e-13
+        assert ref.rel_fro(got, ref.contract(a, ["i", "k"], b, ["k", "j"], ["i", "j"])) <= tol, kind
