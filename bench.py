@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--perm-e", type=int, default=32, help="extent of label e in --workload permute")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="per offered rate in the serving sweep")
     ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--serve-pool", type=int, default=4096, help="distinct requests of the serving workload")
     return ap.parse_args()
 
 
@@ -226,10 +227,13 @@ def barrier(ws):
 
 
 # ----------------------------------------------------------------------------- serving
-def _device_requests(n, seed, dev, flops_hi=1e10, mem_cap=24 << 30):
+def _device_requests(n, seed, dev, flops_hi=1e10, req_cap=128 << 20, mem_cap=48 << 30):
     """Serving-form requests with device-resident operands (shapes from the
-    seeded generator, values from a seeded device generator). Requests are
-    drawn until n are collected within `mem_cap` bytes in total."""
+    seeded generator, values from a seeded device generator). Requests whose
+    operands and output exceed `req_cap` bytes (mostly outer products whose
+    output is gigabytes for few flops) are redrawn; drawing stops at n
+    requests or when the next one would pass `mem_cap` bytes in total.
+    Returns the requests and the draw statistics."""
     import torch
 
     import muscle_gb300 as m
@@ -239,57 +243,85 @@ def _device_requests(n, seed, dev, flops_hi=1e10, mem_cap=24 << 30):
     gen = torch.Generator(device=dev)
     gen.manual_seed(seed)
     tdt = {np.complex128: torch.complex128, np.float64: torch.float64, np.complex64: torch.complex64}
-    out, used = [], 0
+    out, used, draws, flops_drawn = [], 0, 0, []
     while len(out) < n:
         sa, ia, sb, ib, ic, dt, fl = wl.serve_request(rng, 1e4, flops_hi)
+        draws += 1
+        flops_drawn.append(fl)
         ext = dict(zip(ia + ib, sa + sb))
         t = tdt[dt]
-        nbytes = (np.prod(sa) + np.prod(sb) + np.prod([ext[i] for i in ic])) * torch.empty((), dtype=t).element_size()
-        if used + nbytes > mem_cap:
+        nbytes = int(np.prod(sa) + np.prod(sb) + np.prod([ext[i] for i in ic])) * torch.empty((), dtype=t).element_size()
+        if nbytes > req_cap:
             continue
+        if used + nbytes > mem_cap:
+            break
         used += nbytes
         A = m.Tensor(torch.randn(list(reversed(sa)), dtype=t, device=dev, generator=gen).permute(*reversed(range(len(sa)))), ia)
         B = m.Tensor(torch.randn(list(reversed(sb)), dtype=t, device=dev, generator=gen).permute(*reversed(range(len(sb)))), ib)
         C = m.Tensor(m.empty_colmajor([ext[i] for i in ic], t, dev), ic)
         out.append((A, B, C, fl))
     torch.cuda.synchronize(dev)
-    return out
+    stats = {"draws": draws, "redrawn": draws - len(out), "request_cap_bytes": req_cap, "pool_bytes": used,
+             "flops_mean_of_all_draws": float(np.mean(flops_drawn))}
+    return out, stats
 
 
-def serve_bench(dev, rates, seconds, n_requests=192, seed=5, budget=120 * 10**9, quick=False):
-    """One-at-a-time plain launches versus the served stream (continuous
-    batching, emulated and plain forms) under Poisson arrivals."""
+def serve_bench(dev, rates, seconds, n_requests=4096, seed=5, budget=120 * 10**9, quick=False, streams=4,
+                max_batch=256):
+    """Serving form: a Poisson stream of distinct seeded requests (each with
+    its own operands and output; the backlog stays below the pool size, so
+    no two requests in flight share a buffer) served by the continuous
+    batching server in the emulated and the plain form, against
+    one-at-a-time launches of the same request sequence in each form."""
     import torch
 
     import muscle_gb300 as m
+    from muscle_gb300 import _lib
 
-    reqs = _device_requests(n_requests, seed, dev, mem_cap=(16 << 30) if quick else (48 << 30))
-    res = {"requests_in_pool": len(reqs), "flops_mean": float(np.mean([r[3] for r in reqs]))}
-    # one at a time, plain form: launch, wait, next
+    def progress(msg):
+        print(f"[serve {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+    reqs, draw = _device_requests(n_requests, seed, dev, mem_cap=(24 << 30) if quick else (48 << 30))
+    progress(f"{len(reqs)} requests generated")
+    res = {"requests_in_pool": len(reqs), "flops_mean": float(np.mean([r[3] for r in reqs])),
+           "flops_median": float(np.median([r[3] for r in reqs])), "draws": draw, "streams": streams,
+           "max_batch": max_batch}
     plans = {}
     for form in ("plain", "auto"):
         plans[form] = [m.contraction_plan(A.data, A.inds, B.data, B.inds, C.data, C.inds, form) for A, B, C, _ in reqs]
     ws = torch.empty(max(max(p.workspace_bytes for p in plans["auto"]), 1), dtype=torch.uint8, device=dev)
-    from muscle_gb300 import _lib
-
     lib = _lib.load()
     st = torch.cuda.current_stream(dev).cuda_stream
-    t0 = time.perf_counter()
-    n_done = 0
-    while time.perf_counter() - t0 < (0.5 if quick else 2.0) or n_done < 16:
-        A, B, C, _ = reqs[n_done % len(reqs)]
-        p = plans["plain"][n_done % len(reqs)]
-        _lib.check(lib.mgb_contract(p.handle, A.data.data_ptr(), B.data.data_ptr(), C.data.data_ptr(),
-                                    ws.data_ptr(), ws.numel(), st), lib)
-        torch.cuda.synchronize(dev)
-        n_done += 1
-    serial = n_done / (time.perf_counter() - t0)
-    res["one_at_a_time_plain_per_s"] = serial
+
+    def one_at_a_time(form, budget_s):
+        """Launch, wait, next: the same request sequence the server is offered."""
+        t0 = time.perf_counter()
+        n_done = 0
+        while time.perf_counter() - t0 < budget_s or n_done < 8:
+            i = n_done % len(reqs)
+            A, B, C, _ = reqs[i]
+            p = plans[form][i]
+            _lib.check(lib.mgb_contract(p.handle, A.data.data_ptr(), B.data.data_ptr(), C.data.data_ptr(),
+                                        ws.data_ptr(), ws.numel(), st), lib)
+            torch.cuda.synchronize(dev)
+            n_done += 1
+        return n_done / (time.perf_counter() - t0), n_done
+
+    serial = {}
+    for form in ("auto", "plain"):
+        rate, cnt = one_at_a_time(form, 0.5 if quick else 2.0)
+        serial[form] = {"per_s": rate, "requests": cnt}
+        progress(f"one at a time, {form}: {rate:.1f}/s over {cnt} requests")
+    res["one_at_a_time"] = {"emulated_per_s": serial["auto"]["per_s"], "plain_per_s": serial["plain"]["per_s"],
+                            "requests_timed": {"emulated": serial["auto"]["requests"],
+                                               "plain": serial["plain"]["requests"]},
+                            "sequence": "requests 0, 1, 2, ... of the pool, the order the server is offered"}
+    backlog_cap = len(reqs) - 2 * streams * max_batch  # requests in flight never share an output
     sweeps = []
     for form in ("auto", "plain"):
-        # the native FP64 form saturates two orders of magnitude earlier
+        # the native FP64 form saturates far earlier
         form_rates = rates if form == "auto" else [r / 50.0 for r in rates]
-        with m.Server(budget_bytes=budget, streams=4, max_batch=64, form=form, device=dev) as srv:
+        with m.Server(budget_bytes=budget, streams=streams, max_batch=max_batch, form=form, device=dev) as srv:
             for rate in form_rates:
                 srv.reset_stats()
                 rng = np.random.default_rng(seed + int(rate))
@@ -303,8 +335,8 @@ def serve_bench(dev, rates, seconds, n_requests=192, seed=5, budget=120 * 10**9,
                         break
                     if now < t_next:
                         continue
-                    if sent % 256 == 0 and sent - srv.stats()["completed"] > 4096:
-                        overloaded = True  # backlog beyond 4096 requests: stop offering
+                    if sent % 64 == 0 and sent - srv.stats()["completed"] > backlog_cap:
+                        overloaded = True  # backlog near the pool size: stop offering
                         break
                     i = sent % len(reqs)
                     A, B, C, _ = reqs[i]
@@ -312,20 +344,36 @@ def serve_bench(dev, rates, seconds, n_requests=192, seed=5, budget=120 * 10**9,
                     sent += 1
                     t_next += rng.exponential(1.0 / rate)
                 for q in pend:
-                    q.wait()
+                    q.wait(timeout=120.0)  # raises when a request does not finish
                 elapsed = time.perf_counter() - t_start
                 sts = srv.stats()
+                progress(f"{form} at {rate}/s: {sent} sent, {sts['completed']} completed, p99 {sts['p99_ms']:.2f} ms, "
+                         f"{sts['batches']} batches")
                 flops = sum(reqs[k % len(reqs)][3] for k in range(sent))
+                offered_elapsed = min(seconds, elapsed)
+                done_rate = sts["completed"] / elapsed
                 sweeps.append({"form": "emulated" if form == "auto" else "plain", "offered_per_s": rate,
+                               "submitted_per_s": sent / offered_elapsed, "completed_per_s": done_rate,
                                "overloaded": overloaded,
-                               "submitted_per_s": sent / seconds, "completed_per_s": sts["completed"] / elapsed,
+                               "unsaturated": (not overloaded) and done_rate >= 0.95 * rate,
                                "tflops": flops / elapsed / 1e12, "p50_ms": sts["p50_ms"], "p99_ms": sts["p99_ms"],
-                               "batches": sts["batches"]})
+                               "max_ms": sts["max_ms"], "batches": sts["batches"], "requests": sent})
     res["sweep"] = sweeps
-    best = max((x for x in sweeps if x["form"] == "emulated" and not x["overloaded"]),
-               key=lambda x: x["completed_per_s"], default=sweeps[0])
-    res["served_emulated_best"] = best
-    res["served_vs_one_at_a_time_plain"] = best["completed_per_s"] / serial
+
+    def best(form):
+        ok = [x for x in sweeps if x["form"] == form and x["unsaturated"]]
+        return max(ok, key=lambda x: x["completed_per_s"]) if ok else None
+
+    res["served_emulated_best"] = best("emulated") or max(
+        (x for x in sweeps if x["form"] == "emulated"), key=lambda x: x["completed_per_s"])
+    res["served_plain_best"] = best("plain") or max(
+        (x for x in sweeps if x["form"] == "plain"), key=lambda x: x["completed_per_s"])
+    e, p = res["served_emulated_best"], res["served_plain_best"]
+    res["ratios"] = {
+        "served_emulated_vs_one_at_a_time_plain": e["completed_per_s"] / serial["plain"]["per_s"],
+        "served_emulated_vs_one_at_a_time_emulated": e["completed_per_s"] / serial["auto"]["per_s"],
+        "served_plain_vs_one_at_a_time_plain": p["completed_per_s"] / serial["plain"]["per_s"],
+        "basis": "highest unsaturated offered rate of each form (completed >= 95 % of offered, no backlog stop)"}
     return res
 
 
@@ -754,7 +802,7 @@ def main():
             res = hadamard_case(dev, args.steps, args.warmup)
             metric = "hadamard (broadcast product) GB/s"
         else:
-            res = serve_bench(dev, [1000, 3000, 10000, 30000, 100000], args.serve_seconds)
+            res = serve_bench(dev, [1000, 3000, 10000, 30000, 100000], args.serve_seconds, n_requests=args.serve_pool)
             metric = "served contractions/s with p50/p99 ms (Poisson arrivals)"
         if rank == 0:
             print(json.dumps({"metric": metric, "workload": args.workload, "n_gpus": ws, **res}), flush=True)
@@ -964,7 +1012,7 @@ def main():
     # served mixed-size stream (short sweep; the full one is --workload serve)
     del cset, a_f, b_f
     torch.cuda.empty_cache()
-    serving = serve_bench(dev, [1000, 10000, 100000], 1.0, n_requests=64, quick=True)
+    serving = serve_bench(dev, [1000, 3000, 10000, 30000, 100000], 1.0, n_requests=2048, quick=True)
 
     cpu = None
     if rank == 0 and ws == 1:
@@ -995,8 +1043,9 @@ def main():
                         "p99_ms": serving["served_emulated_best"]["p99_ms"],
                         "completed_per_s": serving["served_emulated_best"]["completed_per_s"],
                         "offered_per_s": serving["served_emulated_best"]["offered_per_s"],
-                        "one_at_a_time_plain_per_s": serving["one_at_a_time_plain_per_s"],
-                        "ratio_vs_one_at_a_time_plain": serving["served_vs_one_at_a_time_plain"],
+                        "one_at_a_time": serving["one_at_a_time"],
+                        "ratios": serving["ratios"],
+                        "requests_in_pool": serving["requests_in_pool"],
                         "sweep": serving["sweep"]},
             "gpu_launches": launches_per_step * args.steps,
             "device_status": status,
