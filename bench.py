@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--native-steps", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "peps", "serve", "config2", "kernel", "permute", "hadamard", "unary"],
+                    choices=["precision", "peps", "serve", "config2", "kernel", "permute", "hadamard", "unary", "fp64"],
                     help="precision: the headline line; peps / serve: batching and serving forms; config2: "
                          "plain shapes that permute; kernel / permute: one contraction of the precision "
                          "workload at --n / the permutation of A(a,b,c,d,e) with e = --perm-e (profiling cases); "
@@ -375,6 +375,40 @@ def serve_bench(dev, rates, seconds, n_requests=4096, seed=5, budget=120 * 10**9
         "served_plain_vs_one_at_a_time_plain": p["completed_per_s"] / serial["plain"]["per_s"],
         "basis": "highest unsaturated offered rate of each form (completed >= 95 % of offered, no backlog stop)"}
     return res
+
+
+def fp64_peaks(dev, target_ms=40.0):
+    """Measured FP64 pipe rates of this GPU (the library's roofline probes):
+    DMMA (mma.sync m16n8k16 .f64), DFMA and DADD, each the best over a few
+    grid shapes, every launch sized to about `target_ms`."""
+    import torch
+
+    from muscle_gb300 import _lib
+
+    lib = _lib.load()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    scratch = torch.empty(sms * 16 * 1024 * 8, dtype=torch.uint8, device=dev)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    out = {"sms": sms}
+    import ctypes
+
+    for op, name in ((0, "dmma_tflops"), (1, "dfma_tflops"), (2, "dadd_tflops")):
+        best = 0.0
+        for blocks_per_sm, threads in ((1, 128), (2, 256), (4, 256), (8, 256)):
+            blocks = sms * blocks_per_sm
+            iters = 64
+            r = ctypes.c_double(0.0)
+            _lib.check(lib.mgb_probe_fp64(op, iters, blocks, threads, scratch.data_ptr(), scratch.numel(), st,
+                                          ctypes.byref(r)), lib)
+            # flops of one iteration of the grid, and iterations for target_ms at the first rate
+            per_iter = (blocks * threads / 32 * 4 * 4096) if op == 0 else blocks * threads * 8 * (2 if op == 1 else 1)
+            iters = int(max(64, r.value * 1e12 * target_ms / 1e3 / per_iter))
+            _lib.check(lib.mgb_probe_fp64(op, iters, blocks, threads, scratch.data_ptr(), scratch.numel(), st,
+                                          ctypes.byref(r)), lib)
+            best = max(best, r.value)
+        out[name] = best
+    out["how"] = "tight loops of independent chains, CUDA events, best of 1/2/4/8 blocks per SM"
+    return out
 
 
 def _group_phases_ms(dev, g, steps):
@@ -798,6 +832,9 @@ def main():
         elif args.workload == "unary":
             res = unary_case(dev, args.steps, args.warmup)
             metric = "unary_einsum partial sums GB/s"
+        elif args.workload == "fp64":
+            res = fp64_peaks(dev)
+            metric = "measured FP64 pipe rates (roofline probes)"
         elif args.workload == "hadamard":
             res = hadamard_case(dev, args.steps, args.warmup)
             metric = "hadamard (broadcast product) GB/s"
@@ -917,6 +954,7 @@ def main():
     traffic = ncu_traffic(S)
 
     native = flops / (native_ms / 1e3) / 1e12
+    fp64 = fp64_peaks(dev, target_ms=20.0)
     step()
     torch.cuda.synchronize()
     rel_err = rel(C, Cn)
@@ -1029,7 +1067,8 @@ def main():
             "rel_err": rel_err, "rel_err_reference": "plain FP64 DMMA result on the same inputs",
             "rel_err_vs_exact": exact_check,
             "slice_sweep": sweep, "float32_variant": f32,
-            "native": {"value": native, "unit": "TFLOP/s", "ms_per_step": native_ms, "form": "plain FP64 DMMA (4M)"},
+            "native": {"value": native, "unit": "TFLOP/s", "ms_per_step": native_ms, "form": "plain FP64 DMMA (4M)",
+                       "fp64_peaks_measured": fp64, "frac_of_dmma_peak": native / fp64["dmma_tflops"]},
             "speedup_vs_native": value / native,
             "e2e": {"value": e2e, "unit": "TFLOP/s", "ms_per_step": e2e_ms / args.steps,
                     "h2d_bytes_per_step": A.numel() * 16 + B.numel() * 16, "d2h_bytes_per_step": C.numel() * 16,

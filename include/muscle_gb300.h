@@ -286,6 +286,16 @@ int mgb_device_status(void *stream, int32_t *status);
  * word and the kernel returns normally, so the context stays usable. Read the
  * word with mgb_device_status afterwards.                                  */
 int mgb_selftest_wait_timeout(void *stream);
+/* Roofline probe (no counterpart in the reference): the measured rate of an
+ * FP64 pipe of the current device, the denominator of the plain form's and
+ * the double-precision memory kernels' roofline fractions. op 0 = DMMA
+ * (mma.sync m16n8k16 .f64, 4096 flops per warp instruction), 1 = DFMA (two
+ * flops), 2 = DADD (one flop). Runs `iters` iterations of independent chains
+ * in every thread of `blocks` x `threads` (a multiple of 32), timed with CUDA
+ * events on `stream` (synchronised), and returns TFLOP/s. `scratch` (device,
+ * one double per thread) receives values that keep the work alive.        */
+int mgb_probe_fp64(int32_t op, int64_t iters, int32_t blocks, int32_t threads, void *scratch,
+                   uint64_t scratch_bytes, void *stream, double *tflops);
 /* Library version string. */
 const char *mgb_version(void);
 

@@ -276,15 +276,24 @@ static bool retire(mgb_server_s *s, size_t k) {
         b.mapped = true;
         progressed = true;
     }
-    // one by one: requests whose own launch has completed
+    // one by one: requests whose own launch has completed (the requests of
+    // one variant share its event: each event is queried once per sweep)
     std::vector<std::pair<Req, int32_t>> done;
+    std::vector<std::pair<cudaEvent_t, cudaError_t>> seen;
+    auto query = [&](cudaEvent_t e) {
+        for (auto &x : seen)
+            if (x.first == e) return x.second;
+        const cudaError_t q = cudaEventQuery(e);
+        seen.push_back({e, q});
+        return q;
+    };
     auto sweep = [&](std::vector<Req> &v) {
         std::vector<Req> keep;
         for (auto &r : v) {
-            cudaError_t q = r.done ? cudaEventQuery(r.done) : cudaErrorNotReady;
+            cudaError_t q = r.done ? query(r.done) : cudaErrorNotReady;
             // own events of plain launches and re-runs: their status snapshot
             // is taken at the batch's end
-            if (q == cudaSuccess && r.own_done && cudaEventQuery(b.end) == cudaErrorNotReady) q = cudaErrorNotReady;
+            if (q == cudaSuccess && r.own_done && query(b.end) == cudaErrorNotReady) q = cudaErrorNotReady;
             if (q == cudaErrorNotReady) {
                 keep.push_back(r);
                 continue;

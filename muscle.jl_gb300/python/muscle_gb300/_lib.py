@@ -125,6 +125,7 @@ SIGNATURES = {
     "mgb_device_status": (_i32, [_vp, _P(_i32)]),
     "mgb_selftest_wait_timeout": (_i32, [_vp]),
     "mgb_version": (ctypes.c_char_p, []),
+    "mgb_probe_fp64": (_i32, [_i32, ctypes.c_int64, _i32, _i32, _vp, _u64, _vp, _P(ctypes.c_double)]),
 }
 
 _lock = threading.Lock()

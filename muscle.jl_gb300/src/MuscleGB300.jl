@@ -2,12 +2,12 @@
     MuscleGB300
 
 A Muscle.jl backend for device-resident tensors on NVIDIA GB300 (sm_103a).
-`enable!()` registers `BackendGB300` as the backend for `binary_einsum`,
-`binary_einsum!`, `unary_einsum`, `unary_einsum!`, `hadamard` and `hadamard!`
-on `(DomainCUDA, ...)` operands (the rule tables of
+Loading it routes `binary_einsum`, `binary_einsum!`, `unary_einsum`,
+`unary_einsum!`, `hadamard` and `hadamard!` on CuArray-backed tensors to
+`BackendGB300` by adding methods beside the rule tables of
 src/Operations/binary_einsum.jl:20-31, src/Operations/unary_einsum.jl:20-24
-and src/Operations/hadamard.jl:4-5); the methods `ccall` into
-`libmuscle_gb300.so` (C ABI in include/muscle_gb300.h).
+and src/Operations/hadamard.jl:4-5 (none is replaced); the methods `ccall`
+into `libmuscle_gb300.so` (C ABI in include/muscle_gb300.h).
 `with_backend(f, BackendGB300(...))` selects a form explicitly. `Group` runs
 many independent contractions (a PEPS sweep's site pairs) as a few batched
 launches on one stream. `Server` is the serving loop: contractions submitted
@@ -332,27 +332,43 @@ function Base.close(g::Group)
     return nothing
 end
 
+# ---------------------------------------------------------------------------
+# Routing device-resident operands here without replacing any Muscle method.
+#  * binary_einsum / binary_einsum!: the rules of src/Operations/binary_einsum.jl:21,30
+#    select BackendCuTENSOR, whose CUDA extension defines only 6-argument
+#    methods (ext/MuscleCUDAExt.jl:10,22) while the front-ends call the
+#    4-argument ones (src/Operations/binary_einsum.jl:50,68). These are those
+#    missing 4-argument methods, for tensors whose parent is a CuArray.
+#  * unary_einsum / unary_einsum!: the rules select BackendOMEinsum
+#    (src/Operations/unary_einsum.jl:21,24); methods for CuArray-backed tensors
+#    are more specific than the extension's generic ones
+#    (ext/MuscleOMEinsumExt.jl:25,31).
+#  * hadamard / hadamard!: rules for (DomainCUDA, ...) operands are more
+#    specific than the generic (Domain, ...) rules of src/Operations/hadamard.jl:4-5.
+# Every definition below adds a method; none overwrites one, so loading the
+# package is enough and precompilation stays clean.
+const CuTensor = Tensor{<:Any,<:Any,<:CuArray}
+
+Muscle.binary_einsum(::Muscle.BackendCuTENSOR, inds_c, a::CuTensor, b::CuTensor) =
+    Muscle.binary_einsum(BackendGB300(), inds_c, a, b)
+Muscle.binary_einsum!(::Muscle.BackendCuTENSOR, c::CuTensor, a::CuTensor, b::CuTensor) =
+    Muscle.binary_einsum!(BackendGB300(), c, a, b)
+Muscle.unary_einsum(::Muscle.BackendOMEinsum, inds_y, x::CuTensor) = Muscle.unary_einsum(BackendGB300(), inds_y, x)
+Muscle.unary_einsum!(::Muscle.BackendOMEinsum, y::CuTensor, x::CuTensor) = Muscle.unary_einsum!(BackendGB300(), y, x)
+Muscle.choose_backend_rule(::typeof(Muscle.hadamard), ::Muscle.DomainCUDA, ::Muscle.DomainCUDA) = BackendGB300()
+Muscle.choose_backend_rule(::typeof(Muscle.hadamard!), ::Muscle.DomainCUDA, ::Muscle.DomainCUDA, ::Muscle.DomainCUDA) =
+    BackendGB300()
+
 """
     MuscleGB300.enable!()
 
-Make `BackendGB300` the rule for device-resident operands, replacing the
-`BackendCuTENSOR` / `BackendOMEinsum` rules of
-src/Operations/binary_einsum.jl:21,30 and src/Operations/unary_einsum.jl:21,24,
-and the `BackendBase` rules of src/Operations/hadamard.jl:4-5.
-Muscle defines those methods itself, so they are replaced at run time (method
-overwriting is not allowed while a package precompiles). Without this call
-`with_backend(f, BackendGB300())` still selects the backend.
+Checks that `libmuscle_gb300.so` loads and returns its version string. The
+routing of device-resident operands to `BackendGB300` is active as soon as
+the package is loaded (methods added next to Muscle's rules, none replaced);
+`with_backend(f, BackendGB300(form, slices))` selects a form explicitly.
 """
 function enable!()
-    @eval Muscle begin
-        choose_backend_rule(::typeof(binary_einsum), ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
-        choose_backend_rule(::typeof(binary_einsum!), ::DomainCUDA, ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
-        choose_backend_rule(::typeof(unary_einsum), ::DomainCUDA) = $(BackendGB300)()
-        choose_backend_rule(::typeof(unary_einsum!), ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
-        choose_backend_rule(::typeof(hadamard), ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
-        choose_backend_rule(::typeof(hadamard!), ::DomainCUDA, ::DomainCUDA, ::DomainCUDA) = $(BackendGB300)()
-    end
-    return nothing
+    return unsafe_string(ccall((:mgb_version, libmgb), Cstring, ()))
 end
 
 end # module
