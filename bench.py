@@ -355,7 +355,7 @@ def serve_bench(dev, rates, seconds, n_requests=4096, seed=5, budget=120 * 10**9
                 sweeps.append({"form": "emulated" if form == "auto" else "plain", "offered_per_s": rate,
                                "submitted_per_s": sent / offered_elapsed, "completed_per_s": done_rate,
                                "overloaded": overloaded,
-                               "unsaturated": (not overloaded) and done_rate >= 0.95 * rate,
+                               "unsaturated": (not overloaded) and done_rate >= 0.95 * sent / offered_elapsed,
                                "tflops": flops / elapsed / 1e12, "p50_ms": sts["p50_ms"], "p99_ms": sts["p99_ms"],
                                "max_ms": sts["max_ms"], "batches": sts["batches"], "requests": sent})
     res["sweep"] = sweeps
@@ -373,7 +373,8 @@ def serve_bench(dev, rates, seconds, n_requests=4096, seed=5, budget=120 * 10**9
         "served_emulated_vs_one_at_a_time_plain": e["completed_per_s"] / serial["plain"]["per_s"],
         "served_emulated_vs_one_at_a_time_emulated": e["completed_per_s"] / serial["auto"]["per_s"],
         "served_plain_vs_one_at_a_time_plain": p["completed_per_s"] / serial["plain"]["per_s"],
-        "basis": "highest unsaturated offered rate of each form (completed >= 95 % of offered, no backlog stop)"}
+        "basis": "highest unsaturated offered rate of each form (completions keep up with >= 95 % of the "
+                 "submissions, no backlog stop)"}
     return res
 
 
@@ -446,9 +447,12 @@ def _group_phases_ms(dev, g, steps):
     return out
 
 
-def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
-    """Batching form: PEPS-style pairs, one group per element type, autotuned
-    schedule, replayed as one CUDA graph."""
+def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5, quick=False, check=0):
+    """Batching form: PEPS-style pairs, one group per element type, replayed
+    as one CUDA graph whose schedule the autotuner chose on the group's own
+    data. quick: no per-class breakdown, a shorter one-at-a-time sample.
+    check: members whose results are compared with the CPU oracle (the
+    checker) after the timed replays."""
     import torch
 
     import muscle_gb300 as m
@@ -479,29 +483,28 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
         tuner = Autotuner(os.environ.get("MGB_AUTOTUNE_CACHE"), reps=2)
         g = tuner.group(items)
         flops = g.flops
-        by_parts = {}
-        # (branches, persistent): one persistent tensor-core launch per kernel
-        # variant after the pre-passes, or every bucket's own launches
-        for parts, pers in ((1, True), (4, True), (4, False), (8, False)):
-            graph = g.capture(parts, pers)
-            for _ in range(3):
-                graph.replay()
-            torch.cuda.synchronize(dev)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(steps):
-                graph.replay()
-            e1.record()
-            torch.cuda.synchronize(dev)
-            by_parts[(parts, pers)] = e0.elapsed_time(e1) / steps
-            del graph
-        best_parts = min(by_parts, key=by_parts.get)
-        ms = by_parts[best_parts]
+        # the schedule: (branches, persistent) chosen by the autotuner from
+        # the candidates timed on this group; then timed again on its own
+        best_parts, by_parts = tuner.schedule(g)
+        ms = Autotuner.time_schedule(g, best_parts[0], best_parts[1], steps)
         # the persistent form's two phases on their own: pre-passes (and plain
         # buckets), then the persistent tensor-core launches
-        phase_ms = _group_phases_ms(dev, g, steps)
+        phase_ms = {} if quick else _group_phases_ms(dev, g, steps)
         by_class = []
-        if tdt == torch.complex128:
+        errs = []
+        if check:
+            import oracle.muscle_ref as ref  # the checker
+
+            graph = g.capture()
+            graph.replay()
+            torch.cuda.synchronize(dev)
+            del graph
+            for idx in np.linspace(0, len(items) - 1, check).astype(int):
+                C, A, B = items[idx]
+                want = ref.contract(A.data.cpu().numpy(), [i.tag for i in A.inds], B.data.cpu().numpy(),
+                                    [i.tag for i in B.inds], [i.tag for i in C.inds])
+                errs.append(ref.rel_fro(C.data.cpu().numpy(), want))
+        if tdt == torch.complex128 and not quick:
             # every (M, N, K) class as a group of its own: where the time goes
             classes = {}
             for it, (sa, ia, sb, ib, ic) in zip(items, shapes):
@@ -518,8 +521,8 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
                                  "k_blocks_per_ms": kb / ph["persistent_gemm"]})
                 del gc
                 torch.cuda.empty_cache()
-        # one at a time, plain form, on the first 256 instances
-        sub = items[:256]
+        # one at a time, plain form, on the first instances
+        sub = items[:64 if quick else 256]
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         for C, A, B in sub:
@@ -536,7 +539,11 @@ def peps_bench(dev, instances, cap=1 << 22, seed=10000, steps=5):
                     "persistent_phases_ms": phase_ms, "by_class": by_class,
                     "tflops": flops / (ms / 1e3) / 1e12, "contractions_per_s": len(items) / (ms / 1e3),
                     "one_at_a_time_plain_per_s": one, "forms_chosen": forms, "gflop": flops / 1e9,
-                    "distinct_plans": len({id(p) for p in g.plans})}
+                    "distinct_plans": len({id(p) for p in g.plans}),
+                    "schedule_chosen_by": "autotuner (timed)" if by_parts else "autotuner cache"}
+        if errs:
+            out[key]["max_rel_err_vs_oracle"] = max(errs)
+            out[key]["members_checked"] = len(errs)
         del g, items
         torch.cuda.empty_cache()
     return out
@@ -668,9 +675,10 @@ def kernel_case(dev, n, form, slices, steps, warmup, band=0):
             "tflops_alg": p.flops / ((statistics.mean(pre) + ms) / 1e3) / 1e12, "status": m.device_status(dev)}
 
 
-def permute_case(dev, e, steps, warmup):
-    """Permutation of A(a,b,c,d,e) = 64x96x64x48xe ComplexF64 to (b,d,a,c,e), the
-    reordering the host backend stages for the permuting plain shapes."""
+def permute_case(dev, e, steps, warmup, dtype="c64"):
+    """Permutation of A(a,b,c,d,e) = 64x96x64x48xe ComplexF64 (or Float64) to
+    (b,d,a,c,e), the reordering the host backend stages for the permuting
+    plain shapes."""
     import torch
 
     import muscle_gb300 as m
@@ -679,7 +687,8 @@ def permute_case(dev, e, steps, warmup):
     perm = ["b", "d", "a", "c", "e"]
     g = torch.Generator(device=dev)
     g.manual_seed(0)
-    x = torch.randn(list(reversed(ea)), dtype=torch.complex128, device=dev, generator=g).permute(4, 3, 2, 1, 0)
+    tdt = torch.complex128 if dtype == "c64" else torch.float64
+    x = torch.randn(list(reversed(ea)), dtype=tdt, device=dev, generator=g).permute(4, 3, 2, 1, 0)
     X = m.Tensor(x, ia)
     for _ in range(warmup):
         Y = m.permutedims(X, perm)
@@ -692,7 +701,9 @@ def permute_case(dev, e, steps, warmup):
     torch.cuda.synchronize(dev)
     ms = e0.elapsed_time(e1) / steps
     nb = 2 * x.numel() * x.element_size()
-    return {"bytes": nb, "ms": ms, "gbs": nb / (ms / 1e3) / 1e9,
+    _, hbm, kind = peaks()
+    return {"dtype": dtype, "bytes": nb, "ms": ms, "gbs": nb / (ms / 1e3) / 1e9,
+            "frac_of_hbm": nb / (ms / 1e3) / 1e9 / hbm, "peak_kind": kind,
             "bit_exact": bool(torch.equal(Y.data, x.permute(1, 3, 0, 2, 4)))}
 
 
@@ -818,7 +829,7 @@ def main():
     dev = torch.device("cuda", local)
     if args.workload != "precision":
         if args.workload == "peps":
-            res = peps_bench(dev, args.instances)
+            res = peps_bench(dev, args.instances, check=8)
             metric = "PEPS batch: contractions/s and TFLOP/s, one graph-captured group"
         elif args.workload == "config2":
             res = config2_bench(dev)
@@ -827,7 +838,7 @@ def main():
             res = kernel_case(dev, args.n, args.form, args.slices, args.steps, args.warmup, args.band)
             metric = "one contraction of the precision workload (profiling case)"
         elif args.workload == "permute":
-            res = permute_case(dev, args.perm_e, args.steps, args.warmup)
+            res = {d: permute_case(dev, args.perm_e, args.steps, args.warmup, d) for d in ("c64", "f64")}
             metric = "permutation kernel GB/s (profiling case)"
         elif args.workload == "unary":
             res = unary_case(dev, args.steps, args.warmup)
@@ -1047,6 +1058,10 @@ def main():
     e2e_ok = bool(torch.equal(cset[(args.steps - 1) % 2][3].view(n, n), C.t().cpu()))
     status = m.device_status(dev)
 
+    # batching form: a PEPS group of 1024 instances (the full one is --workload peps)
+    peps = peps_bench(dev, 1024, quick=True, check=8)
+    torch.cuda.empty_cache()
+
     # served mixed-size stream (short sweep; the full one is --workload serve)
     del cset, a_f, b_f
     torch.cuda.empty_cache()
@@ -1086,6 +1101,13 @@ def main():
                         "ratios": serving["ratios"],
                         "requests_in_pool": serving["requests_in_pool"],
                         "sweep": serving["sweep"]},
+            "batching": {k: {kk: peps[k][kk] for kk in ("graph_ms", "graph_branches", "persistent", "tflops",
+                                                          "contractions_per_s", "one_at_a_time_plain_per_s",
+                                                          "max_rel_err_vs_oracle", "members_checked", "forms_chosen",
+                                                          "graph_ms_by_branches")}
+                         for k in ("c64", "c32")} | {"instances": peps["instances"],
+                                                     "redraws_per_instance": peps["redraws_per_instance"],
+                                                     "cap_elements": peps["cap_elements"]},
             "gpu_launches": launches_per_step * args.steps,
             "device_status": status,
             "clocks": clk.summary(),

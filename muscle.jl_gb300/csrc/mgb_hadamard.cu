@@ -179,6 +179,56 @@ __global__ void __launch_bounds__(256) k_hadamard_rows_same(const T *__restrict_
     }
 }
 
+// The same with 16-byte vectors (V elements each) when every row of A and C
+// (and of B, unless it is broadcast along the row) starts on a 16-byte
+// boundary: a quarter (4-byte types) or half (8-byte types) of the memory
+// instructions, each moving a full 16 bytes.
+template <typename T, int V>
+__global__ void __launch_bounds__(256, 4) k_hadamard_rows_vec(const T *__restrict__ A, const T *__restrict__ B,
+                                                           T *__restrict__ C, ModeGroup outer, int64_t len,
+                                                           int64_t sb, int64_t rows) {
+    constexpr int U = 4;
+    static_assert(sizeof(T) * V == 16, "16-byte vectors");
+    struct alignas(16) Vec {
+        T v[V];
+    };
+    const int64_t chunks = (len + HCHUNK - 1) / HCHUNK;
+    for (int64_t w = blockIdx.x; w < rows * chunks; w += gridDim.x) {
+        const int64_t r = w / chunks, lo = (w - r * chunks) * HCHUNK, hi = min(len, lo + HCHUNK);
+        const T *a = A + group_offset(outer, 0, r) + lo;
+        const T *b = B + group_offset(outer, 1, r);
+        T *c = C + group_offset(outer, 2, r) + lo;
+        const T y0 = __ldg(b);
+        const int64_t nv = (hi - lo) / V;  // whole vectors of this chunk (lo is a multiple of V)
+        const Vec *av = reinterpret_cast<const Vec *>(a);
+        const Vec *bv = reinterpret_cast<const Vec *>(b + lo);
+        Vec *cv = reinterpret_cast<Vec *>(c);
+        for (int64_t i0 = threadIdx.x; i0 < nv; i0 += (int64_t)U * blockDim.x) {
+            Vec x[U], y[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int64_t i = i0 + (int64_t)u * blockDim.x;
+                if (i < nv) {
+                    x[u] = av[i];
+                    if (sb != 0) y[u] = bv[i];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int64_t i = i0 + (int64_t)u * blockDim.x;
+                if (i < nv) {
+                    Vec z;
+#pragma unroll
+                    for (int e = 0; e < V; ++e) z.v[e] = HVal<T>::mul(x[u].v[e], sb != 0 ? y[u].v[e] : y0);
+                    cv[i] = z;
+                }
+            }
+        }
+        for (int64_t i = nv * V + threadIdx.x; i < hi - lo; i += blockDim.x)
+            c[i] = HVal<T>::mul(__ldg(a + i), sb != 0 ? __ldg(b + lo + i) : y0);
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_hadamard_flat(HArgs a, ModeGroup g, int64_t total) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
@@ -203,9 +253,24 @@ static int run_hadamard(const ModeGroup &g, const HArgs &a, cudaStream_t s) {
         const int64_t rows = outer.size();
         const int dt = HDtype<T>::code;
         const int64_t items = rows * ((g.ext[0] + HCHUNK - 1) / HCHUNK);
-        if (a.ta == dt && a.tb == dt && a.tc == dt && g.str[0][0] == 1)
-            k_hadamard_rows_same<T><<<(unsigned)std::min(items, cap * 4), 256, 0, s>>>(
-                (const T *)a.A, (const T *)a.B, (T *)a.C, outer, g.ext[0], g.str[1][0], rows);
+        const bool same = a.ta == dt && a.tb == dt && a.tc == dt && g.str[0][0] == 1;
+        // 16-byte vectors: every row of A and C (and of B unless broadcast)
+        // starts on a 16-byte boundary
+        bool vec = same && sizeof(T) < 16 && (g.str[1][0] == 0 || g.str[1][0] == 1);
+        if (vec) {
+            auto al = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
+            vec = al(a.A) && al(a.C) && (g.str[1][0] == 0 || al(a.B));
+            for (int i = 0; i < outer.n && vec; ++i)
+                vec = (outer.str[0][i] * (int64_t)sizeof(T)) % 16 == 0 && (outer.str[2][i] * (int64_t)sizeof(T)) % 16 == 0 &&
+                      (g.str[1][0] == 0 || (outer.str[1][i] * (int64_t)sizeof(T)) % 16 == 0);
+        }
+        const unsigned grid = (unsigned)std::min(items, cap * 4);
+        if (vec)
+            k_hadamard_rows_vec<T, 16 / sizeof(T)><<<grid, 256, 0, s>>>((const T *)a.A, (const T *)a.B, (T *)a.C, outer,
+                                                                        g.ext[0], g.str[1][0], rows);
+        else if (same)
+            k_hadamard_rows_same<T><<<grid, 256, 0, s>>>((const T *)a.A, (const T *)a.B, (T *)a.C, outer, g.ext[0],
+                                                        g.str[1][0], rows);
         else
             k_hadamard_rows<T><<<(unsigned)std::min(rows, cap * 4), 256, 0, s>>>(a, outer, g.ext[0], g.str[0][0],
                                                                                g.str[1][0], g.str[2][0], rows);

@@ -279,13 +279,35 @@ __device__ __forceinline__ int bexp_of(float v) { return bexp((double)v); }
 __device__ __forceinline__ int bexp_of(float2 v) { return max(bexp((double)v.x), bexp((double)v.y)); }
 
 // `emax` (nullable): also the largest exponent of the whole operand.
+// 2^(2 d) as a float (0 below 2^-126)
+__device__ __forceinline__ float pow4f(int d) { return d >= -63 ? __int_as_float((127 + 2 * d) << 23) : 0.f; }
+
 struct ScaleSmem {
     int64_t roff[32], koff[32];
     int red[8][33];
+    int cmax[8][33];    // partials: per-warp column maxima
+    float csum[8][33];  // partials: per-warp column sums
 };
+
+// |x|^2 4^-(t - 1023), from the exponent and the top of the mantissa, for an
+// element whose biased exponent is at most t (zero, subnormal and non-finite
+// elements give 0: negligible, or flagged through the exponent table)
+__device__ __forceinline__ float sq_tile(double x, int t) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const int be = (int)((b >> 52) & 0x7FF);
+    if (be == 0 || be == 0x7FF) return 0.f;
+    const float f = __int_as_float(0x3F800000 | (uint32_t)((b >> 29) & 0x7FFFFF));
+    return f * f * pow4f(be - t);
+}
+__device__ __forceinline__ float sq_tile(double2 x, int t) { return sq_tile(x.x, t) + sq_tile(x.y, t); }
+__device__ __forceinline__ float sq_tile(float x, int t) { return sq_tile((double)x, t); }
+__device__ __forceinline__ float sq_tile(float2 x, int t) { return sq_tile((double)x.x, t) + sq_tile((double)x.y, t); }
 template <typename T>
+// `part` (nullable, adaptive plans): per 32-row tile and k, the tile's
+// largest exponent t and the sum of |x|^2 4^-(t - 1023) over its rows,
+// at part[(l * ceil(R / 32) + tile) * K + k].
 __device__ __forceinline__ void oz_scale_tile(const T *__restrict__ X, const OpGeom &g, int32_t *exps,
-                                              int32_t *emax, int64_t blk, int64_t l, ScaleSmem &sm) {
+                                              int32_t *emax, int2 *part, int64_t blk, int64_t l, ScaleSmem &sm) {
     int64_t tiles_k = (g.K + 31) / 32;
     int64_t tr = blk / tiles_k, tk = blk - tr * tiles_k;
     int64_t r0 = tr * 32, k0 = tk * 32;
@@ -294,20 +316,65 @@ __device__ __forceinline__ void oz_scale_tile(const T *__restrict__ X, const OpG
     else if (tid < 64) sm.koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
     const T *Xl = g.ptrs ? (const T *)g.ptrs[l] : X + group_offset(g.gl, g.t, l);
     __syncthreads();
-    if (g.rows_fast) {
+    const int64_t R32 = (g.R + 31) / 32;
+    int2 *pt = part ? part + (l * R32 + tr) * g.K + k0 : nullptr;  // this tile's partials
+    if (g.rows_fast) {  // lanes walk rows
         int e = 0;
         int64_t r = r0 + tx;
-        for (int kk = ty; kk < 32; kk += 8)
-            if (r < g.R && k0 + kk < g.K) e = max(e, bexp_of(__ldg(Xl + sm.roff[tx] + sm.koff[kk])));
+        for (int kk = ty; kk < 32; kk += 8) {
+            const bool in = r < g.R && k0 + kk < g.K;
+            T v;
+            int be = 0;
+            if (in) {
+                v = __ldg(Xl + sm.roff[tx] + sm.koff[kk]);
+                be = bexp_of(v);
+                e = max(e, be);
+            }
+            if (pt) {
+                int t = be;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) t = max(t, __shfl_xor_sync(0xffffffffu, t, d));
+                float q = in ? sq_tile(v, t) : 0.f;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) q += __shfl_xor_sync(0xffffffffu, q, d);
+                if (tx == 0 && k0 + kk < g.K) pt[kk] = make_int2(t, __float_as_int(q));
+            }
+        }
         sm.red[ty][tx] = e;
-    } else {
+    } else {  // lanes walk k
+        T v[4];
+        int be4[4];
+#pragma unroll
         for (int j = 0; j < 4; ++j) {
             int rr = ty + 8 * j;
-            int e = 0;
-            if (r0 + rr < g.R && k0 + tx < g.K) e = bexp_of(__ldg(Xl + sm.roff[rr] + sm.koff[tx]));
+            be4[j] = 0;
+            if (r0 + rr < g.R && k0 + tx < g.K) {
+                v[j] = __ldg(Xl + sm.roff[rr] + sm.koff[tx]);
+                be4[j] = bexp_of(v[j]);
+            }
+            int e = be4[j];
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, d));
             if (tx == 0) sm.red[j][rr] = e;  // rows rr = ty + 8 j are distinct per (ty, j)
+        }
+        if (pt) {
+            sm.cmax[ty][tx] = max(max(be4[0], be4[1]), max(be4[2], be4[3]));
+            __syncthreads();
+            int t = 0;
+#pragma unroll
+            for (int y = 0; y < 8; ++y) t = max(t, sm.cmax[y][tx]);
+            float q = 0.f;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (be4[j] > 0) q += sq_tile(v[j], t);
+            sm.csum[ty][tx] = q;
+            __syncthreads();
+            if (ty == 0 && k0 + tx < g.K) {
+                float s2 = 0.f;
+#pragma unroll
+                for (int y = 0; y < 8; ++y) s2 += sm.csum[y][tx];
+                pt[tx] = make_int2(t, __float_as_int(s2));
+            }
         }
     }
     __syncthreads();
@@ -329,9 +396,10 @@ __device__ __forceinline__ void oz_scale_tile(const T *__restrict__ X, const OpG
     }
 }
 template <typename T>
-__global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps, int32_t *emax) {
+__global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps, int32_t *emax,
+                                                  int2 *part) {
     __shared__ ScaleSmem sm;
-    oz_scale_tile<T>(X, g, exps, emax, blockIdx.x, blockIdx.y, sm);
+    oz_scale_tile<T>(X, g, exps, emax, part, blockIdx.x, blockIdx.y, sm);
 }
 
 // =============================================================================
@@ -362,84 +430,58 @@ struct OzStats {
 };
 static_assert(sizeof(OzStats) == 64, "stats header");
 
-// 2^(2 d) as a float (0 below 2^-126)
-__device__ __forceinline__ float pow4f(int d) { return d >= -63 ? __int_as_float((127 + 2 * d) << 23) : 0.f; }
 
-// |x|^2 4^-(be_max + 1 - 1023), from the exponent and the top of the mantissa
-__device__ __forceinline__ float sq_rel(double x, int be_max) {
-    const uint64_t b = (uint64_t)__double_as_longlong(x);
-    const int be = (int)((b >> 52) & 0x7FF);
-    if (be == 0 || be == 0x7FF) return 0.f;  // zero / subnormal (negligible), non-finite (flagged)
-    const float f = __int_as_float(0x3F800000 | (uint32_t)((b >> 29) & 0x7FFFFF));
-    return f * f * pow4f(be - be_max - 1);
-}
-__device__ __forceinline__ float sq_rel(double2 x, int be_max) { return sq_rel(x.x, be_max) + sq_rel(x.y, be_max); }
-__device__ __forceinline__ float sq_rel(float x, int be_max) { return sq_rel((double)x, be_max); }
-__device__ __forceinline__ float sq_rel(float2 x, int be_max) { return sq_rel((double)x.x, be_max) + sq_rel((double)x.y, be_max); }
 
-// Per k: q[l][k] += sum over the block's rows of |x|^2 relative to the
-// operand's largest exponent; the blocks of the first k tile also add the
-// rows' squared scales to P[l] and flag non-finite rows.
+// Statistics of one operand from the exponent scan's partials, once the
+// operand's largest exponent is known. Blocks [0, ceil(K / 256)) of batch
+// entry l write q[l][k], the squared norm of column k relative to 4^(be_max
+// + 1 - 1023); the blocks after them add the rows' squared scales
+// 4^(be_i - be_max) to P[l] and flag non-finite rows.
 struct StatSmem {
-    int64_t roff[32], koff[32];
-    float sq[32];
-    float sp;
+    float red[32];
 };
-template <typename T>
-__device__ __forceinline__ void oz_stat_tile(const T *__restrict__ X, const OpGeom &g,
-                                             const int32_t *__restrict__ exps, OzStats *st, int t, float *q,
-                                             float *P, int64_t blk, int64_t l, StatSmem &sm) {
+__device__ __forceinline__ void oz_stat_block(const int2 *__restrict__ part, const int32_t *__restrict__ exps,
+                                              OzStats *st, int t, float *q, float *P, int64_t R, int64_t K,
+                                              int64_t blk, int64_t l, StatSmem &sm) {
     const int be_max = st->emax[t];
-    int64_t tiles_k = (g.K + 31) / 32;
-    int64_t tr = blk / tiles_k, tk = blk - tr * tiles_k;
-    int64_t r0 = tr * 32, k0 = tk * 32;
-    int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
-    if (tid < 32) {
-        sm.roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
-        sm.sq[tid] = 0.f;
-        if (tid == 0) sm.sp = 0.f;
-    } else if (tid < 64) {
-        sm.koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
+    const int64_t nq = (K + 255) / 256, R32 = (R + 31) / 32;
+    if (blk < nq) {
+        const int64_t k = blk * 256 + threadIdx.x;
+        if (k < K) {
+            const int2 *p = part + l * R32 * K + k;
+            float acc = 0.f;
+            for (int64_t tr = 0; tr < R32; ++tr) {
+                const int2 v = __ldg(p + tr * K);
+                const float x = __int_as_float(v.y);
+                if (x != 0.f) acc += x * pow4f(v.x - be_max - 1);
+            }
+            q[l * K + k] = acc;
+        }
+        return;
     }
-    const T *Xl = g.ptrs ? (const T *)g.ptrs[l] : X + group_offset(g.gl, g.t, l);
-    __syncthreads();
-    if (g.rows_fast) {  // lanes walk rows: reduce over the warp per k
-        const int64_t r = r0 + tx;
-        for (int kk = ty; kk < 32; kk += 8) {
-            float v = (r < g.R && k0 + kk < g.K) ? sq_rel(__ldg(Xl + sm.roff[tx] + sm.koff[kk]), be_max) : 0.f;
+    const int64_t i = (blk - nq) * 256 + threadIdx.x;
+    float w = 0.f;
+    if (i < R) {
+        const int be = exps[l * R + i];
+        if (be == 0x7FF) st->nonfinite = 1;
+        else if (be > 0) w = pow4f(be - be_max);
+    }
 #pragma unroll
-            for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-            if (tx == 0) atomicAdd(&sm.sq[kk], v);
-        }
-    } else {  // lanes walk k
-        float v = 0.f;
-        for (int j = 0; j < 4; ++j) {
-            const int rr = ty + 8 * j;
-            if (r0 + rr < g.R && k0 + tx < g.K) v += sq_rel(__ldg(Xl + sm.roff[rr] + sm.koff[tx]), be_max);
-        }
-        atomicAdd(&sm.sq[tx], v);
-    }
-    if (tk == 0 && tid < 32) {
-        float w = 0.f;
-        if (r0 + tid < g.R) {
-            const int be = exps[l * g.R + r0 + tid];
-            if (be == 0x7FF) st->nonfinite = 1;
-            else if (be > 0) w = pow4f(be - be_max);
-        }
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) w += __shfl_xor_sync(0xffffffffu, w, d);
-        if (tid == 0) sm.sp = w;
-    }
+    for (int d = 16; d > 0; d >>= 1) w += __shfl_xor_sync(0xffffffffu, w, d);
+    if (threadIdx.x % 32 == 0) sm.red[threadIdx.x / 32] = w;
     __syncthreads();
-    if (tid < 32 && k0 + tid < g.K && sm.sq[tid] != 0.f) atomicAdd(q + l * g.K + k0 + tid, sm.sq[tid]);
-    if (tid == 0 && tk == 0 && sm.sp != 0.f) atomicAdd(P + l, sm.sp);
+    if (threadIdx.x == 0) {
+        float s2 = 0.f;
+        for (int y = 0; y < (int)blockDim.x / 32; ++y) s2 += sm.red[y];
+        if (s2 != 0.f) atomicAdd(P + l, s2);
+    }
 }
-template <typename T>
-__global__ void __launch_bounds__(256) k_oz_stat(const T *__restrict__ X, OpGeom g, const int32_t *__restrict__ exps,
-                                                 OzStats *st, int t, float *q, float *P) {
+__global__ void __launch_bounds__(256) k_oz_stat(const int2 *__restrict__ part, const int32_t *__restrict__ exps,
+                                                 OzStats *st, int t, float *q, float *P, int64_t R, int64_t K) {
     __shared__ StatSmem sm;
-    oz_stat_tile<T>(X, g, exps, st, t, q, P, blockIdx.x, blockIdx.y, sm);
+    oz_stat_block(part, exps, st, t, q, P, R, K, blockIdx.x, blockIdx.y, sm);
 }
+__host__ __device__ inline int64_t oz_stat_blocks(int64_t R, int64_t K) { return (K + 255) / 256 + (R + 255) / 256; }
 
 // One block: the error estimate of every candidate slice count (bit S of
 // `cand`) and the choice, the smallest count within `tol`, else 0 (plain).
@@ -1265,10 +1307,14 @@ void ozaki_setup(ContractionPlan &p) {
         off = align256(off + (uint64_t)p.L * p.N * 4);
         p.oz_R = oz_fits(p.k_e, S) ? 0 : -1;  // -1: K too long for the exact accumulator
         if (p.adaptive) {
-            // OzStats, P_A[L], P_B[L], q_A[L][K], q_B[L][K]
+            // OzStats, P_A[L], P_B[L], q_A[L][K], q_B[L][K] (cleared every
+            // call), then the exponent scan's partials of A and B
+            // ([L][ceil(R / 32)][K] pairs, every one written every call)
             p.ws_stat = off;
             off = align256(off + sizeof(OzStats) + 2 * (uint64_t)p.L * 4);
             off = align256(off + 2 * (uint64_t)p.L * p.K * 4);
+            off = align256(off + (uint64_t)p.L * ((p.M + 31) / 32) * p.K * 8);
+            off = align256(off + (uint64_t)p.L * ((p.N + 31) / 32) * p.K * 8);
         }
     }
     p.ws_bytes = off;
@@ -1278,6 +1324,7 @@ void ozaki_setup(ContractionPlan &p) {
 struct OzStatArea {
     OzStats *st;
     float *pa, *pb, *qa, *qb;
+    int2 *parta, *partb;
 };
 static OzStatArea stat_area(const ContractionPlan &p, void *ws) {
     OzStatArea a;
@@ -1285,8 +1332,13 @@ static OzStatArea stat_area(const ContractionPlan &p, void *ws) {
     a.st = (OzStats *)w;
     a.pa = (float *)(w + sizeof(OzStats));
     a.pb = a.pa + p.L;
-    a.qa = (float *)((uint8_t *)ws + align256(p.ws_stat + sizeof(OzStats) + 2 * (uint64_t)p.L * 4));
+    uint64_t off = align256(p.ws_stat + sizeof(OzStats) + 2 * (uint64_t)p.L * 4);
+    a.qa = (float *)((uint8_t *)ws + off);
     a.qb = a.qa + p.L * p.K;
+    off = align256(off + 2 * (uint64_t)p.L * p.K * 4);
+    a.parta = (int2 *)((uint8_t *)ws + off);
+    off = align256(off + (uint64_t)p.L * ((p.M + 31) / 32) * p.K * 8);
+    a.partb = (int2 *)((uint8_t *)ws + off);
     return a;
 }
 static uint64_t stat_bytes(const ContractionPlan &p) {
@@ -1436,26 +1488,23 @@ static int run_prepass(const OpGeom &g, int mode, const void *X, int32_t *exps, 
 
 template <typename T>
 static int run_scale(const OpGeom &g, const void *X, int32_t *exps, int64_t L, cudaStream_t s,
-                     int32_t *emax = nullptr) {
+                     int32_t *emax = nullptr, int2 *part = nullptr) {
     int64_t tiles = ((g.R + 31) / 32) * ((g.K + 31) / 32);
     if (tiles > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the scale grid");
     dim3 grid((unsigned)tiles, (unsigned)L);
-    k_oz_scale<T><<<grid, 256, 0, s>>>((const T *)X, g, exps, emax);
+    k_oz_scale<T><<<grid, 256, 0, s>>>((const T *)X, g, exps, emax, part);
     MGB_CUDA_CHECK(cudaGetLastError());
     return MGB_OK;
 }
 
-template <typename T>
-static int run_stat(const OpGeom &g, const void *X, const int32_t *exps, OzStats *st, int t, float *q, float *P,
-                    int64_t L, cudaStream_t s) {
-    int64_t tiles = ((g.R + 31) / 32) * ((g.K + 31) / 32);
-    if (tiles > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the statistics grid");
-    dim3 grid((unsigned)tiles, (unsigned)L);
-    k_oz_stat<T><<<grid, 256, 0, s>>>((const T *)X, g, exps, st, t, q, P);
+static int run_stat(const int2 *part, const int32_t *exps, OzStats *st, int t, float *q, float *P, int64_t R,
+                    int64_t K, int64_t L, cudaStream_t s) {
+    const int64_t blocks = oz_stat_blocks(R, K);
+    if (blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the statistics grid");
+    k_oz_stat<<<dim3((unsigned)blocks, (unsigned)L), 256, 0, s>>>(part, exps, st, t, q, P, R, K);
     MGB_CUDA_CHECK(cudaGetLastError());
     return MGB_OK;
 }
-
 // Calls f with a null pointer of the operand's element type.
 template <typename F>
 static int by_type(int dtype, F &&f) {
@@ -1502,19 +1551,15 @@ int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *
             sel = &sa_.st->sel;
         }
         int32_t *emax_a = p.adaptive ? &sa_.st->emax[0] : nullptr, *emax_b = p.adaptive ? &sa_.st->emax[1] : nullptr;
-        st = by_type(p.a.dtype, [&](auto tag) { return run_scale<TypeOf<decltype(tag)>>(ga, A, ea, p.L, s, emax_a); });
+        st = by_type(p.a.dtype,
+                     [&](auto tag) { return run_scale<TypeOf<decltype(tag)>>(ga, A, ea, p.L, s, emax_a, sa_.parta); });
         if (st) return st;
-        st = by_type(p.b.dtype, [&](auto tag) { return run_scale<TypeOf<decltype(tag)>>(gb, B, eb, p.L, s, emax_b); });
+        st = by_type(p.b.dtype,
+                     [&](auto tag) { return run_scale<TypeOf<decltype(tag)>>(gb, B, eb, p.L, s, emax_b, sa_.partb); });
         if (st) return st;
         if (p.adaptive) {
-            st = by_type(p.a.dtype, [&](auto tag) {
-                return run_stat<TypeOf<decltype(tag)>>(ga, A, ea, sa_.st, 0, sa_.qa, sa_.pa, p.L, s);
-            });
-            if (st) return st;
-            st = by_type(p.b.dtype, [&](auto tag) {
-                return run_stat<TypeOf<decltype(tag)>>(gb, B, eb, sa_.st, 1, sa_.qb, sa_.pb, p.L, s);
-            });
-            if (st) return st;
+            if ((st = run_stat(sa_.parta, ea, sa_.st, 0, sa_.qa, sa_.pa, p.M, p.K, p.L, s))) return st;
+            if ((st = run_stat(sa_.partb, eb, sa_.st, 1, sa_.qb, sa_.pb, p.N, p.K, p.L, s))) return st;
             // Fluctuations of a Frobenius norm over few outputs: a margin that
             // vanishes for large results.
             const double margin = 1.0 + 2.0 / std::sqrt((double)std::max<int64_t>(p.M * p.N * p.L, 1));
@@ -1723,6 +1768,7 @@ struct PreJob {
     const int32_t *sel; // adaptive choice of the contraction, or null
     OzStats *st;        // its statistics (adaptive) or null
     float *q, *P;       // this operand's per-k norms and squared scales
+    int2 *part;         // the exponent scan's partials of this operand (adaptive) or null
     void *zero[2];      // regions cleared by PRE_ZERO (exponents; statistics for t == 0)
     int64_t zero_words[2];
     int64_t tiles[PRE_PHASES];  // blocks of every phase
@@ -1793,18 +1839,13 @@ __global__ void __launch_bounds__(256, 4) k_oz_pre_multi(const PreJob *__restric
     const int64_t l = local / per_l, blk = local - l * per_l;
     if (phase == PRE_SCALE) {
         switch (J.dtype) {
-        case MGB_F64: oz_scale_tile<double>((const double *)J.X, J.g, J.exps, J.emax, blk, l, sm.scale); break;
-        case MGB_C64: oz_scale_tile<double2>((const double2 *)J.X, J.g, J.exps, J.emax, blk, l, sm.scale); break;
-        case MGB_F32: oz_scale_tile<float>((const float *)J.X, J.g, J.exps, J.emax, blk, l, sm.scale); break;
-        default: oz_scale_tile<float2>((const float2 *)J.X, J.g, J.exps, J.emax, blk, l, sm.scale); break;
+        case MGB_F64: oz_scale_tile<double>((const double *)J.X, J.g, J.exps, J.emax, J.part, blk, l, sm.scale); break;
+        case MGB_C64: oz_scale_tile<double2>((const double2 *)J.X, J.g, J.exps, J.emax, J.part, blk, l, sm.scale); break;
+        case MGB_F32: oz_scale_tile<float>((const float *)J.X, J.g, J.exps, J.emax, J.part, blk, l, sm.scale); break;
+        default: oz_scale_tile<float2>((const float2 *)J.X, J.g, J.exps, J.emax, J.part, blk, l, sm.scale); break;
         }
     } else if (phase == PRE_STAT) {
-        switch (J.dtype) {
-        case MGB_F64: oz_stat_tile<double>((const double *)J.X, J.g, J.exps, J.st, J.t, J.q, J.P, blk, l, sm.stat); break;
-        case MGB_C64: oz_stat_tile<double2>((const double2 *)J.X, J.g, J.exps, J.st, J.t, J.q, J.P, blk, l, sm.stat); break;
-        case MGB_F32: oz_stat_tile<float>((const float *)J.X, J.g, J.exps, J.st, J.t, J.q, J.P, blk, l, sm.stat); break;
-        default: oz_stat_tile<float2>((const float2 *)J.X, J.g, J.exps, J.st, J.t, J.q, J.P, blk, l, sm.stat); break;
-        }
+        oz_stat_block(J.part, J.exps, J.st, J.t, J.q, J.P, J.g.R, J.g.K, blk, l, sm.stat);
     } else {
         int S = J.S;
         if (J.sel) {
@@ -1907,6 +1948,7 @@ static void fill_prejob(PreJob &J, const ContractionPlan &p, int t, const void *
             J.emax = &a.st->emax[t];
             J.q = t == 0 ? a.qa : a.qb;
             J.P = t == 0 ? a.pa : a.pb;
+            J.part = t == 0 ? a.parta : a.partb;
             if (t == 0) {
                 J.zero[1] = a.st;
                 J.zero_words[1] = (int64_t)(stat_bytes(p) / 4);
@@ -1917,7 +1959,7 @@ static void fill_prejob(PreJob &J, const ContractionPlan &p, int t, const void *
     J.tiles[PRE_ZERO] = zw ? std::min<int64_t>((zw + 1023) / 1024, 64) : 0;
     const int64_t tiles32 = ((R + 31) / 32) * ((K + 31) / 32) * L;
     J.tiles[PRE_SCALE] = exact ? tiles32 : 0;
-    J.tiles[PRE_STAT] = (exact && p.adaptive) ? tiles32 : 0;
+    J.tiles[PRE_STAT] = (exact && p.adaptive) ? oz_stat_blocks(R, K) * L : 0;
     J.tiles[PRE_SLICE] = ((R + 31) / 32) * ((K + KT - 1) / KT) * L;
 }
 

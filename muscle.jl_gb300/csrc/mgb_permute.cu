@@ -4,9 +4,10 @@
 // After folding, the copy is one of:
 //  * row copy   — the fastest mode of Y is also unit-stride in X: contiguous
 //                 rows, copied with 128-bit vectors when aligned;
-//  * transpose  — X and Y have different unit-stride modes: 64x64 (32x32 for
-//                 16-byte types) shared-memory tiles, coalesced on both
-//                 sides, other modes enumerated by the grid;
+//  * transpose  — X and Y have different unit-stride modes: shared-memory
+//                 tiles with edges of 32 or 64 elements (32 x 32 for 16-byte
+//                 types), coalesced on both sides, other modes enumerated by
+//                 the grid;
 //  * gather     — strided views without a unit-stride mode: element-wise.
 // HBM-bound: algorithmic bytes = numel * (sizeof(src) + sizeof(dst)).
 #include <algorithm>
@@ -78,11 +79,14 @@ __global__ void k_rowcopy(const TS *__restrict__ x, TD *__restrict__ y, ModeGrou
 }
 
 // ---- tiled transpose ------------------------------------------------------------
-template <typename TS, typename TD, int T>
+// TA x TB tiles: TA elements along a (Y's unit-stride mode) by TB along b
+// (X's unit-stride mode); loads walk b and stores walk a, 32 consecutive
+// elements per warp on both sides.
+template <typename TS, typename TD, int TA, int TB>
 __global__ void k_transpose(const TS *__restrict__ x, TD *__restrict__ y, ModeGroup outer,
                             int64_t ea, int64_t eb, int64_t sxa, int64_t syb, int64_t tiles_a,
                             int64_t tiles_b) {
-    __shared__ TD tile[T][T + 1];
+    __shared__ TD tile[TA][TB + 1];
     int64_t blk = blockIdx.x;
     int64_t tb = blk % tiles_b;
     blk /= tiles_b;
@@ -90,23 +94,77 @@ __global__ void k_transpose(const TS *__restrict__ x, TD *__restrict__ y, ModeGr
     int64_t o = blk / tiles_a;
     const TS *xo = x + group_offset(outer, 0, o);
     TD *yo = y + group_offset(outer, 1, o);
-    int64_t a0 = ta * T, b0 = tb * T;
+    int64_t a0 = ta * TA, b0 = tb * TB;
     int tx = threadIdx.x % 32, ty = threadIdx.x / 32;  // 32 x 8
 #pragma unroll
-    for (int bb = 0; bb < T; bb += 32) {
+    for (int bb = 0; bb < TB; bb += 32) {
 #pragma unroll
-        for (int r = ty; r < T; r += 8) {
+        for (int r = ty; r < TA; r += 8) {
             int64_t ia = a0 + r, ib = b0 + bb + tx;
             if (ia < ea && ib < eb) tile[r][bb + tx] = Conv<TS, TD>::f(__ldg(xo + ia * sxa + ib));
         }
     }
     __syncthreads();
 #pragma unroll
-    for (int aa = 0; aa < T; aa += 32) {
+    for (int aa = 0; aa < TA; aa += 32) {
 #pragma unroll
-        for (int r = ty; r < T; r += 8) {
+        for (int r = ty; r < TB; r += 8) {
             int64_t ib = b0 + r, ia = a0 + aa + tx;
             if (ia < ea && ib < eb) yo[ia + ib * syb] = tile[aa + tx][r];
+        }
+    }
+}
+
+// Same-type 8-byte elements (Float64, ComplexF32) with 16-byte vectors on both
+// sides: 64 x 64 tiles, each lane loads two consecutive elements of X's
+// unit-stride mode and stores two consecutive elements of Y's, so every
+// global access moves 16 bytes (scalar accesses only at ragged edges). Used
+// when every tile row starts on a 16-byte boundary in X and in Y.
+template <typename T>
+__global__ void __launch_bounds__(256) k_transpose_v2(const T *__restrict__ x, T *__restrict__ y, ModeGroup outer,
+                                                      int64_t ea, int64_t eb, int64_t sxa, int64_t syb,
+                                                      int64_t tiles_a, int64_t tiles_b) {
+    static_assert(sizeof(T) == 8, "8-byte elements");
+    struct alignas(16) P2 {
+        T v[2];
+    };
+    __shared__ T tile[64][65];
+    int64_t blk = blockIdx.x;
+    const int64_t tb = blk % tiles_b;
+    blk /= tiles_b;
+    const int64_t ta = blk % tiles_a;
+    const int64_t o = blk / tiles_a;
+    const T *xo = x + group_offset(outer, 0, o);
+    T *yo = y + group_offset(outer, 1, o);
+    const int64_t a0 = ta * 64, b0 = tb * 64;
+    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+    const int c = 2 * lane;  // this lane's pair within a tile row
+#pragma unroll
+    for (int r = w; r < 64; r += 8) {
+        const int64_t ia = a0 + r, ib = b0 + c;
+        if (ia >= ea) continue;
+        const T *src = xo + ia * sxa + ib;
+        if (ib + 1 < eb) {
+            const P2 v = *reinterpret_cast<const P2 *>(src);
+            tile[r][c] = v.v[0];
+            tile[r][c + 1] = v.v[1];
+        } else if (ib < eb) {
+            tile[r][c] = __ldg(src);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = w; r < 64; r += 8) {
+        const int64_t ib = b0 + r, ia = a0 + c;
+        if (ib >= eb) continue;
+        T *dst = yo + ia + ib * syb;
+        if (ia + 1 < ea) {
+            P2 v;
+            v.v[0] = tile[c][r];
+            v.v[1] = tile[c + 1][r];
+            *reinterpret_cast<P2 *>(dst) = v;
+        } else if (ia < ea) {
+            *dst = tile[c][r];
         }
     }
 }
@@ -167,12 +225,41 @@ static int run_permute(const PermGeom &pg, const TS *x, TD *y, cudaStream_t s) {
         ModeGroup outer = drop_mode(g, 0, pg.b);
         int64_t ea = g.ext[0], eb = g.ext[pg.b];
         int64_t sxa = g.str[0][0], syb = g.str[1][pg.b];
-        constexpr int T = sizeof(TD) <= 8 ? 64 : 32;  // 32 KB (8-byte) or 16 KB (16-byte) tiles
-        int64_t tiles_a = (ea + T - 1) / T, tiles_b = (eb + T - 1) / T;
+        // Tile edges of 32 or 64 elements, each chosen to pad its extent
+        // least (a 96-wide panel is three 32-row tiles, not one and a half
+        // 64-row ones whose second half idles), larger on ties; 16-byte
+        // types stay at 32 x 32 (16 KB of shared memory).
+        if constexpr (std::is_same<TS, TD>::value && sizeof(TD) == 8) {
+            // 16-byte vectors: every tile row starts on a 16-byte boundary in
+            // X (row stride sxa, tile columns from an even b) and in Y
+            bool al = ((uintptr_t)x % 16 == 0) && ((uintptr_t)y % 16 == 0) && sxa % 2 == 0 && syb % 2 == 0;
+            for (int i = 0; i < outer.n && al; ++i) al = outer.str[0][i] % 2 == 0 && outer.str[1][i] % 2 == 0;
+            if (al) {
+                const int64_t tiles_a = (ea + 63) / 64, tiles_b = (eb + 63) / 64;
+                const int64_t blocks = tiles_a * tiles_b * outer.size();
+                if (blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "permute: too many tiles");
+                k_transpose_v2<TD><<<(unsigned)blocks, 256, 0, s>>>((const TD *)x, y, outer, ea, eb, sxa, syb, tiles_a,
+                                                                     tiles_b);
+                MGB_CUDA_CHECK(cudaGetLastError());
+                return MGB_OK;
+            }
+        }
+        auto pad = [](int64_t e, int64_t t) { return (e + t - 1) / t * t; };
+        const bool wide = sizeof(TD) <= 8;
+        const int ta_ = (wide && pad(ea, 64) <= pad(ea, 32)) ? 64 : 32;
+        const int tb_ = (wide && pad(eb, 64) <= pad(eb, 32)) ? 64 : 32;
+        int64_t tiles_a = (ea + ta_ - 1) / ta_, tiles_b = (eb + tb_ - 1) / tb_;
         int64_t blocks = tiles_a * tiles_b * outer.size();
         if (blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "permute: too many tiles");
-        k_transpose<TS, TD, T><<<(unsigned)blocks, 256, 0, s>>>(x, y, outer, ea, eb, sxa, syb,
-                                                               tiles_a, tiles_b);
+        const unsigned nb = (unsigned)blocks;
+        if (ta_ == 64 && tb_ == 64)
+            k_transpose<TS, TD, 64, 64><<<nb, 256, 0, s>>>(x, y, outer, ea, eb, sxa, syb, tiles_a, tiles_b);
+        else if (ta_ == 64)
+            k_transpose<TS, TD, 64, 32><<<nb, 256, 0, s>>>(x, y, outer, ea, eb, sxa, syb, tiles_a, tiles_b);
+        else if (tb_ == 64)
+            k_transpose<TS, TD, 32, 64><<<nb, 256, 0, s>>>(x, y, outer, ea, eb, sxa, syb, tiles_a, tiles_b);
+        else
+            k_transpose<TS, TD, 32, 32><<<nb, 256, 0, s>>>(x, y, outer, ea, eb, sxa, syb, tiles_a, tiles_b);
     } else {
         int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 32);
         k_gather<TS, TD><<<(unsigned)blocks, 256, 0, s>>>(x, y, g, total);

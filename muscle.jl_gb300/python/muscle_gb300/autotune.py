@@ -1,15 +1,19 @@
 """Autotuner for grouped contractions.
 
-For each shape class of a group (members that share a plan signature) it
-times the candidate schedules - arithmetic form (the emulated form of the
-element type, or the native one; both meet the precision target) and the
-rasterisation band of the tensor-core kernel - on the group's own data, keeps
-the fastest, and caches the decision in a JSON file keyed by device name,
-element type and shape. Later groups with the same classes reuse the cached
-choice without timing.
+Two decisions, each timed on the group's own data and cached in a JSON file
+keyed by device name, element types and shapes (later groups with the same
+classes reuse the cached choice without timing):
+  * per shape class (members that share a plan signature): the arithmetic
+    form (the emulated form of the element type, or the native one; both
+    meet the precision target) and the rasterisation band of the
+    tensor-core kernel;
+  * per group: the schedule of the whole group as a CUDA graph - one
+    persistent tensor-core launch per kernel variant after every pre-pass,
+    or every bucket's own launches, on 1, 4 or 8 parallel branches.
 """
 from __future__ import annotations
 
+import hashlib
 import json
 import os
 import threading
@@ -20,6 +24,8 @@ from .grouped import Group
 
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "muscle_gb300", "autotune.json")
 BANDS = (1, 2, 4)  # 2, 3, 8 row tiles per band
+# (parallel graph branches, one persistent launch per kernel variant)
+SCHEDULES = ((1, True), (4, True), (4, False), (8, False))
 
 
 def _class_key(c, a, b) -> str:
@@ -99,3 +105,45 @@ class Autotuner:
     def group(self, items) -> Group:
         forms, bands = self.tune(items)
         return Group(items, forms, bands=bands)
+
+    @staticmethod
+    def time_schedule(group: Group, parts: int, persistent: bool, reps: int) -> float:
+        """Milliseconds per replay of the group captured with this schedule."""
+        graph = group.capture(parts, persistent)
+        for _ in range(2):
+            graph.replay()
+        torch.cuda.synchronize(group.device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            graph.replay()
+        e1.record()
+        torch.cuda.synchronize(group.device)
+        del graph
+        return e0.elapsed_time(e1) / reps
+
+    def schedule(self, group: Group):
+        """Chooses (parts, persistent) for the group, sets it as the group's
+        default schedule and returns it with the time of every candidate
+        (milliseconds per replay; empty when the choice came from the cache)."""
+        counts = {}
+        for c, a, b in group.items:
+            k = _class_key(c, a, b)
+            counts[k] = counts.get(k, 0) + 1
+        sig = "\n".join(f"{k}#{n}" for k, n in sorted(counts.items()))
+        key = "schedule|" + hashlib.sha1((sig + "|" + "|".join(group.forms)).encode()).hexdigest()
+        with self.lock:
+            hit = self.cache.get(key)
+        times = {}
+        if hit is None:
+            for parts, pers in SCHEDULES:
+                times[(parts, pers)] = self.time_schedule(group, parts, pers, self.reps)
+            parts, pers = min(times, key=times.get)
+            with self.lock:
+                self.cache[key] = {"parts": parts, "persistent": pers, "ms": times[(parts, pers)],
+                                   "members": len(group.items)}
+                self._save()
+        else:
+            parts, pers = hit["parts"], hit["persistent"]
+        group.schedule = (parts, pers)
+        return (parts, pers), times

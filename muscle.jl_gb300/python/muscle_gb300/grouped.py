@@ -53,6 +53,9 @@ class Group:
         self.workspace = torch.empty(max(self.workspace_bytes, 1), dtype=torch.uint8, device=self.device)
         if bands is not None:
             self.set_bands(bands)
+        # default schedule of capture(): every bucket's own launches on four
+        # parallel branches (the autotuner measures and replaces it)
+        self.schedule = (4, False)
 
     def _pointer_arrays(self):
         n = len(self.items)
@@ -120,7 +123,7 @@ class Group:
             self._side = cache
         return cache
 
-    def capture(self, parts: int = 1, persistent: bool = True) -> torch.cuda.CUDAGraph:
+    def capture(self, parts: int | None = None, persistent: bool | None = None) -> torch.cuda.CUDAGraph:
         """Warm up once (which also uploads the persistent launches' job
         tables), then record execute() into a CUDA graph (with parts > 1 the
         parts become parallel branches of the graph).
@@ -128,7 +131,13 @@ class Group:
         On a 4096-member PEPS batch (148 plans) parts=4, persistent=False was
         the fastest schedule on GB300 (ComplexF64 116 ms against 141 ms for
         one persistent launch after all pre-passes): the HBM-bound pre-passes
-        of some buckets then overlap the tensor-core work of others."""
+        of some buckets then overlap the tensor-core work of others. Without
+        arguments the group's `schedule` is used (set by
+        ``Autotuner.schedule``)."""
+        if parts is None:
+            parts = self.schedule[0]
+        if persistent is None:
+            persistent = self.schedule[1]
         s = torch.cuda.Stream(self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):

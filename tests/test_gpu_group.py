@@ -142,3 +142,30 @@ def test_autotuner_caches_choices(tmp_path):
     again = Autotuner(path, reps=1)
     forms, bands = again.tune(items)  # served from the cache, no timing
     assert all(f in ("ozaki", "plain") for f in forms)
+
+
+def test_autotuner_chooses_and_caches_the_schedule(tmp_path):
+    """The group schedule (parallel branches, one persistent launch or every
+    bucket's own launches) is timed on the group's data, kept as the group's
+    default for capture(), cached, and every schedule gives the same result."""
+    import json
+
+    from muscle_gb300.autotune import SCHEDULES, Autotuner
+
+    insts = instances(24, 1400, np.complex128)
+    items = make_items(insts)
+    path = str(tmp_path / "tune.json")
+    tuner = Autotuner(path, reps=1)
+    g = tuner.group(items)
+    chosen, times = tuner.schedule(g)
+    assert chosen in SCHEDULES and set(times) == set(SCHEDULES) and g.schedule == chosen
+    assert times[chosen] == min(times.values())
+    graph = g.capture()
+    graph.replay()
+    torch.cuda.synchronize()
+    for (C, _, _), (a, ia, b, ib, ic) in zip(items, insts):
+        assert ref.rel_fro(C.data.cpu().numpy(), ref.contract(a, ia, b, ib, ic)) <= 1e-13
+    assert any(k.startswith("schedule|") for k in json.load(open(path)))
+    g2 = Autotuner(path, reps=1).group(items)
+    again, t2 = Autotuner(path, reps=1).schedule(g2)
+    assert again == chosen and t2 == {}  # from the cache, no timing
