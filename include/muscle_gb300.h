@@ -286,6 +286,28 @@ int mgb_device_status(void *stream, int32_t *status);
  * word and the kernel returns normally, so the context stays usable. Read the
  * word with mgb_device_status afterwards.                                  */
 int mgb_selftest_wait_timeout(void *stream);
+/* ---- thin singular value decomposition ---------------------------------------
+ * The factorisation of simple_update (src/Operations/simple_update.jl:56-60),
+ * done on the host by LinearAlgebra.svd in tensor_svd_thin
+ * (src/Operations/tensor_svd.jl:98-125) and on CUDA by cuTensorNet (:34).
+ * A (m x n, column-major with leading dimension lda, Float64 or ComplexF64)
+ * = U diag(s) V^H with k = min(m, n) and s descending (Float64). Writes the
+ * first `keep` triplets (keep <= 0 or > k: all k): U m x keep, s keep, V
+ * n x keep, column-major and dense. Flags: MGB_SVD_NORMALIZE scales the kept
+ * s to unit 2-norm (normalize! of simple_update); MGB_SVD_CONJ_V writes
+ * conj(V), the right factor as tensor_svd_thin labels it; MGB_SVD_SQRT_S
+ * writes sqrt of the (normalised) s, for an equal absorb. One-sided Jacobi
+ * rotations in one thread block on the device: min(m, n) <= 1024, m n <=
+ * 2^28. Left vectors of exactly zero singular values are completed to an
+ * orthonormal set. The workspace comes from mgb_svd_workspace_size.        */
+#define MGB_SVD_NORMALIZE 1
+#define MGB_SVD_CONJ_V 2
+#define MGB_SVD_SQRT_S 4
+int mgb_svd_workspace_size(int32_t dtype, int64_t m, int64_t n, uint64_t *bytes);
+int mgb_svd(int32_t dtype, int64_t m, int64_t n, const void *A, int64_t lda, void *U, void *s,
+            void *V, int32_t keep, int32_t flags, void *workspace, uint64_t workspace_bytes,
+            void *stream);
+
 /* Roofline probe (no counterpart in the reference): the measured rate of an
  * FP64 pipe of the current device, the denominator of the plain form's and
  * the double-precision memory kernels' roofline fractions. op 0 = DMMA

@@ -34,6 +34,8 @@ from .ops import (
     device_status,
     hadamard,
     hadamard_,
+    simple_update,
+    tensor_svd_thin,
     permutedims,
     promote_eltype,
     unary_einsum,

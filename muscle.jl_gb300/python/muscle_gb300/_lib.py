@@ -28,6 +28,7 @@ ERR_NOT_FINITE = 8
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 F32, F64, C32, C64 = 0, 1, 2, 3
+SVD_NORMALIZE, SVD_CONJ_V, SVD_SQRT_S = 1, 2, 4
 FORM_AUTO, FORM_PLAIN, FORM_OZAKI, FORM_BF16X3 = 0, 1, 2, 3
 
 FORMS = {"auto": FORM_AUTO, "plain": FORM_PLAIN, "ozaki": FORM_OZAKI, "bf16x3": FORM_BF16X3}
@@ -126,6 +127,9 @@ SIGNATURES = {
     "mgb_selftest_wait_timeout": (_i32, [_vp]),
     "mgb_version": (ctypes.c_char_p, []),
     "mgb_probe_fp64": (_i32, [_i32, ctypes.c_int64, _i32, _i32, _vp, _u64, _vp, _P(ctypes.c_double)]),
+    "mgb_svd_workspace_size": (_i32, [_i32, ctypes.c_int64, ctypes.c_int64, _P(_u64)]),
+    "mgb_svd": (_i32, [_i32, ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int64, _vp, _vp, _vp, _i32, _i32, _vp,
+                       _u64, _vp]),
 }
 
 _lock = threading.Lock()

@@ -275,9 +275,75 @@ class BackendGB300(Backend):
         return c
 
 
+    # tensor_svd_thin (src/Operations/tensor_svd.jl:98-125) on the device
+    def tensor_svd_thin(self, x: Tensor, inds_u, inds_v, ind_s, keep: int = 0, normalize: bool = False,
+                        sqrt_s: bool = False):
+        """U (inds_u..., ind_s), s (ind_s), conj(V) (inds_v..., ind_s) of the
+        thin SVD of x matricised as [inds_u; inds_v]; keep > 0 keeps the
+        largest `keep` triplets; normalize scales the kept s to unit norm;
+        sqrt_s returns sqrt(s) (for an equal absorb)."""
+        _require_cuda(x.data)
+        inds_u = [i if isinstance(i, Index) else Index(i) for i in inds_u]
+        inds_v = [i if isinstance(i, Index) else Index(i) for i in inds_v]
+        ind_s = ind_s if isinstance(ind_s, Index) else Index(ind_s)
+        if sorted(map(repr, inds_u + inds_v)) != sorted(map(repr, x.inds)):
+            raise ArgumentError("tensor_svd_thin: inds_u and inds_v must split inds(x)")
+        if x.dtype not in (torch.float64, torch.complex128):
+            raise _lib.UnsupportedError("tensor_svd_thin on the device: Float64 or ComplexF64")
+        dense = True
+        acc = 1
+        for d in range(x.data.dim()):
+            dense = dense and (x.data.shape[d] == 1 or x.data.stride(d) == acc)
+            acc *= x.data.shape[d]
+        # the matrix must be dense column-major: permute (copy) otherwise
+        xm = x if (list(x.inds) == inds_u + inds_v and dense) else permutedims(x, inds_u + inds_v)
+        su = [x.size(i) for i in inds_u]
+        sv = [x.size(i) for i in inds_v]
+        m, n = int(torch.tensor(su, dtype=torch.int64).prod()), int(torch.tensor(sv, dtype=torch.int64).prod())
+        k = min(m, n)
+        keep = k if keep <= 0 else min(keep, k)
+        dev = x.data.device
+        lib = _lib.load()
+        wsb = ctypes.c_uint64(0)
+        dt = mgb_dtype(x.dtype)
+        check(lib.mgb_svd_workspace_size(dt, m, n, ctypes.byref(wsb)), lib)
+        ws = torch.empty(max(int(wsb.value), 1), dtype=torch.uint8, device=dev)
+        U = empty_colmajor(su + [keep], x.dtype, dev)
+        S = torch.empty(keep, dtype=torch.float64, device=dev)
+        V = empty_colmajor(sv + [keep], x.dtype, dev)
+        flags = _lib.SVD_CONJ_V | (_lib.SVD_NORMALIZE if normalize else 0) | (_lib.SVD_SQRT_S if sqrt_s else 0)
+        src = xm.data
+        check(lib.mgb_svd(dt, m, n, src.data_ptr(), max(m, 1), U.data_ptr(), S.data_ptr(), V.data_ptr(), keep, flags,
+                          ws.data_ptr(), ws.numel(), _stream_handle(dev)), lib)
+        return Tensor(U, inds_u + [ind_s]), Tensor(S, [ind_s]), Tensor(V, inds_v + [ind_s])
+
+    # simple_update (src/Operations/simple_update.jl:35-82) on the device
+    def simple_update(self, A: Tensor, ind_physical_a, B: Tensor, ind_physical_b, ind_bond_ab, G: Tensor,
+                      ind_physical_g_a, ind_physical_g_b, normalize: bool = False, absorb=None, maxdim=None):
+        idx = lambda i: i if isinstance(i, Index) else Index(i)
+        pa, pb, bond, ga, gb = map(idx, (ind_physical_a, ind_physical_b, ind_bond_ab, ind_physical_g_a,
+                                         ind_physical_g_b))
+        AB = self.binary_einsum(binary_inds_c(A.inds, B.inds, dims=[bond]), A, B)
+        theta = self.binary_einsum(binary_inds_c(AB.inds, G.inds, dims=[pa, pb]), AB, G)
+        theta = Tensor(theta.data, [pa if i == ga else pb if i == gb else i for i in theta.inds])
+        inds_u, inds_v = setdiff(A.inds, [bond]), setdiff(B.inds, [bond])
+        keep = 0 if maxdim is None else int(maxdim)
+        U, S, V = self.tensor_svd_thin(theta, inds_u, inds_v, bond, keep, normalize, sqrt_s=absorb == "equally")
+        if absorb is None:
+            return U, S, V
+        if absorb in ("u", "equally"):
+            self.hadamard_(U, U, S)
+        if absorb in ("v", "equally"):
+            self.hadamard_(V, V, S)
+        if absorb not in ("u", "v", "equally"):
+            raise ArgumentError(f"unknown absorb behaviour {absorb!r}")
+        return U, V
+
+
 for _f, _doms in (("binary_einsum", (DomainCUDA, DomainCUDA)), ("binary_einsum_", (DomainCUDA, DomainCUDA, DomainCUDA)),
                   ("unary_einsum", (DomainCUDA,)), ("unary_einsum_", (DomainCUDA, DomainCUDA)),
-                  ("hadamard", (DomainCUDA, DomainCUDA)), ("hadamard_", (DomainCUDA, DomainCUDA, DomainCUDA))):
+                  ("hadamard", (DomainCUDA, DomainCUDA)), ("hadamard_", (DomainCUDA, DomainCUDA, DomainCUDA)),
+                  ("simple_update", (DomainCUDA, DomainCUDA, DomainCUDA)), ("tensor_svd_thin", (DomainCUDA,))):
     register_rule(_f, _doms, BackendGB300)
 
 
@@ -392,3 +458,29 @@ def device_status(device=None) -> int:
     st = ctypes.c_int32(0)
     check(lib.mgb_device_status(_stream_handle(device or torch.cuda.current_device()), ctypes.byref(st)), lib)
     return int(st.value)
+
+
+def tensor_svd_thin(x: Tensor, inds_u=None, inds_v=None, ind_s=None):
+    """Thin SVD of a tensor (src/Operations/tensor_svd.jl:66-69,98-125):
+    U (inds_u..., ind_s), s (ind_s) and conj(V) (inds_v..., ind_s); either
+    inds_u or inds_v may be omitted (the other labels of x)."""
+    if inds_u is None and inds_v is None:
+        raise ArgumentError("tensor_svd_thin: give inds_u or inds_v")
+    if inds_u is None:
+        inds_u = setdiff(x.inds, _labels(inds_v))
+    if inds_v is None:
+        inds_v = setdiff(x.inds, _labels(inds_u))
+    ind_s = Index("svd") if ind_s is None else ind_s
+    backend = choose_backend(tensor_svd_thin, x.data)
+    return backend.tensor_svd_thin(x, _labels(inds_u), _labels(inds_v), ind_s)
+
+
+def simple_update(A: Tensor, ind_physical_a, B: Tensor, ind_physical_b, ind_bond_ab, G: Tensor, ind_physical_g_a,
+                  ind_physical_g_b, normalize: bool = False, absorb=None, maxdim=None):
+    """Muscle's simple_update (src/Operations/simple_update.jl:16-82): apply
+    the gate G to the pair A, B joined by ind_bond_ab and refactor it: returns
+    (U, s, V), or (U, V) with s absorbed (absorb = "u", "v" or "equally",
+    the reference's AbsorbU / AbsorbV / AbsorbEqually)."""
+    backend = choose_backend(simple_update, A.data, B.data, G.data)
+    return backend.simple_update(A, ind_physical_a, B, ind_physical_b, ind_bond_ab, G, ind_physical_g_a,
+                                 ind_physical_g_b, normalize=normalize, absorb=absorb, maxdim=maxdim)

@@ -333,6 +333,72 @@ function Base.close(g::Group)
 end
 
 # ---------------------------------------------------------------------------
+# tensor_svd_thin (src/Operations/tensor_svd.jl:98-125) and simple_update
+# (src/Operations/simple_update.jl:35-82) on the device: contractions and
+# absorbs through the library, the thin SVD through mgb_svd (one-sided Jacobi)
+
+# permutedims by labels (src/Tensor.jl:316-319) through mgb_permute: a dense
+# column-major copy with labels `to`
+function permute_device(t::Tensor, to)
+    y = Tensor(similar(parent(t), Tuple(size(t, i) for i in to)), collect(to))
+    m = modemap(t)
+    at, ay = descarrays(t, m), descarrays(y, m)
+    GC.@preserve at ay begin
+        check(ccall((:mgb_permute, libmgb), Cint,
+                    (Ref{TensorDesc}, Ref{TensorDesc}, CuPtr{Cvoid}, CuPtr{Cvoid}, CUDA.CUstream),
+                    Ref(desc(t, at)), Ref(desc(y, ay)), parent(t), parent(y), CUDA.stream()))
+    end
+    return y
+end
+
+const SVD_NORMALIZE, SVD_CONJ_V, SVD_SQRT_S = Cint(1), Cint(2), Cint(4)
+
+function svd_device(::BackendGB300, x::Tensor, inds_u, inds_v, ind_s; keep::Integer=0, flags::Cint=SVD_CONJ_V)
+    T = eltype(x)
+    T in (Float64, ComplexF64) || throw(ArgumentError("tensor_svd_thin on the device: Float64 or ComplexF64"))
+    xm = permute_device(x, [inds_u; inds_v])
+    su, sv = [size(x, i) for i in inds_u], [size(x, i) for i in inds_v]
+    m, n = prod(su), prod(sv)
+    k = min(m, n)
+    keep = keep <= 0 ? k : min(keep, k)
+    bytes = Ref{UInt64}(0)
+    check(ccall((:mgb_svd_workspace_size, libmgb), Cint, (Cint, Int64, Int64, Ref{UInt64}), dtype_code(T), m, n, bytes))
+    ws = CuArray{UInt8}(undef, max(bytes[], 1))
+    U = similar(parent(x), T, su..., keep)
+    s = similar(parent(x), Float64, keep)
+    V = similar(parent(x), T, sv..., keep)
+    check(ccall((:mgb_svd, libmgb), Cint,
+                (Cint, Int64, Int64, CuPtr{Cvoid}, Int64, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Cint, Cint,
+                 CuPtr{Cvoid}, UInt64, CUDA.CUstream),
+                dtype_code(T), m, n, parent(xm), max(m, 1), U, s, V, Cint(keep), flags, ws, bytes[], CUDA.stream()))
+    return Tensor(U, [inds_u; ind_s]), Tensor(s, [ind_s]), Tensor(V, [inds_v; ind_s])
+end
+
+function Muscle.tensor_svd_thin(be::BackendGB300, A::Tensor; inds_u=(), inds_v=(), ind_s=Index(gensym(:vind)),
+                                inplace=false, kwargs...)
+    inds_u, inds_v = Muscle.factorinds(inds(A), inds_u, inds_v)
+    return svd_device(be, A, collect(inds_u), collect(inds_v), ind_s)
+end
+
+function Muscle.simple_update(be::BackendGB300, A::Tensor, ind_physical_a::Index, B::Tensor, ind_physical_b::Index,
+                              ind_bond_ab::Index, G::Tensor, ind_physical_g_a::Index, ind_physical_g_b::Index;
+                              normalize::Bool=false, absorb::Muscle.AbsorbBehavior=Muscle.DontAbsorb(),
+                              atol::Float64=0.0, rtol::Float64=0.0, maxdim=nothing)
+    Θ = Muscle.with_backend(be) do
+        Muscle.binary_einsum(Muscle.binary_einsum(A, B; dims=[ind_bond_ab]), G; dims=[ind_physical_a, ind_physical_b])
+    end
+    Θ = replace(Θ, ind_physical_g_a => ind_physical_a, ind_physical_g_b => ind_physical_b)
+    inds_u = setdiff(inds(A), [ind_bond_ab])
+    inds_v = setdiff(inds(B), [ind_bond_ab])
+    flags = SVD_CONJ_V | (normalize ? SVD_NORMALIZE : Cint(0)) | (absorb isa Muscle.AbsorbEqually ? SVD_SQRT_S : Cint(0))
+    U, s, V = svd_device(be, Θ, inds_u, inds_v, ind_bond_ab; keep=something(maxdim, 0), flags)
+    absorb isa Muscle.DontAbsorb && return U, s, V
+    absorb isa Muscle.AbsorbV || Muscle.hadamard!(be, U, U, s)
+    absorb isa Muscle.AbsorbU || Muscle.hadamard!(be, V, V, s)
+    return U, V
+end
+
+# ---------------------------------------------------------------------------
 # Routing device-resident operands here without replacing any Muscle method.
 #  * binary_einsum / binary_einsum!: the rules of src/Operations/binary_einsum.jl:21,30
 #    select BackendCuTENSOR, whose CUDA extension defines only 6-argument
@@ -345,6 +411,9 @@ end
 #    (ext/MuscleOMEinsumExt.jl:25,31).
 #  * hadamard / hadamard!: rules for (DomainCUDA, ...) operands are more
 #    specific than the generic (Domain, ...) rules of src/Operations/hadamard.jl:4-5.
+#  * simple_update: the rule selects BackendCuTensorNet
+#    (src/Operations/simple_update.jl:5); a method for CuArray-backed tensors is
+#    more specific than the extension's (ext/MusclecuTensorNetExt.jl:13).
 # Every definition below adds a method; none overwrites one, so loading the
 # package is enough and precompilation stays clean.
 const CuTensor = Tensor{<:Any,<:Any,<:CuArray}
@@ -355,6 +424,9 @@ Muscle.binary_einsum!(::Muscle.BackendCuTENSOR, c::CuTensor, a::CuTensor, b::CuT
     Muscle.binary_einsum!(BackendGB300(), c, a, b)
 Muscle.unary_einsum(::Muscle.BackendOMEinsum, inds_y, x::CuTensor) = Muscle.unary_einsum(BackendGB300(), inds_y, x)
 Muscle.unary_einsum!(::Muscle.BackendOMEinsum, y::CuTensor, x::CuTensor) = Muscle.unary_einsum!(BackendGB300(), y, x)
+Muscle.simple_update(::Muscle.BackendCuTensorNet, A::CuTensor, pa::Index, B::CuTensor, pb::Index, bond::Index,
+                     G::CuTensor, ga::Index, gb::Index; kwargs...) =
+    Muscle.simple_update(BackendGB300(), A, pa, B, pb, bond, G, ga, gb; kwargs...)
 Muscle.choose_backend_rule(::typeof(Muscle.hadamard), ::Muscle.DomainCUDA, ::Muscle.DomainCUDA) = BackendGB300()
 Muscle.choose_backend_rule(::typeof(Muscle.hadamard!), ::Muscle.DomainCUDA, ::Muscle.DomainCUDA, ::Muscle.DomainCUDA) =
     BackendGB300()

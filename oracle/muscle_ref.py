@@ -15,6 +15,8 @@ Followed reference code (paths inside the Muscle.jl repository, v0.3.20):
                                              (cuTENSOR semantics, ext/MuscleCUDAExt.jl:10-41)
   * unary trace / diagonal / sums .......... src/Operations/unary_einsum.jl:26-46,
                                              test/integration/omeinsum.jl:6-100
+  * simple_update (contract, SVD, absorb) .. src/Operations/simple_update.jl:35-82,
+                                             src/Operations/tensor_svd.jl:98-125
 The GEMM is numpy's matmul, i.e. OpenBLAS (scipy-openblas), the same BLAS
 family Julia's LinearAlgebra uses. Julia arrays are column-major: reshapes
 here use order="F" so that the folded matrices are the same as Julia's.
@@ -208,6 +210,53 @@ def hadamard(a, ia, b, ib):
     if np.iscomplexobj(prod) and not np.iscomplexobj(a) and np.any(np.imag(prod) != 0):
         raise ArgumentError("hadamard: InexactError (complex product into a real array)")
     return np.array(np.real(prod) if not np.iscomplexobj(a) else prod, dtype=a.dtype, order="F"), ia
+
+
+def tensor_svd_thin(x, ix, inds_u, inds_v):
+    """tensor_svd_thin of BackendBase (src/Operations/tensor_svd.jl:98-125):
+    permute to [inds_u; inds_v], reshape to a matrix (column-major), thin SVD
+    (numpy's LAPACK, as Julia's LinearAlgebra.svd), and the factors as tensors:
+    U (inds_u..., s), s, and conj(V) (inds_v..., s)."""
+    ix, inds_u, inds_v = list(ix), list(inds_u), list(inds_v)
+    su = [x.shape[ix.index(i)] for i in inds_u]
+    sv = [x.shape[ix.index(i)] for i in inds_v]
+    xm = _permute(x, ix, inds_u + inds_v).reshape(_prod(su), _prod(sv), order="F")
+    u, s, vh = np.linalg.svd(xm, full_matrices=False)
+    k = s.shape[0]
+    U = np.array(u.reshape(su + [k], order="F"), order="F")
+    Vt = np.array(vh.T.reshape(sv + [k], order="F"), order="F")  # conj(V) = (V^H)^T
+    return U, s, Vt
+
+
+def simple_update(a, ia, phys_a, b, ib, phys_b, bond, g, ig, g_a, g_b, normalize=False, absorb=None, maxdim=None):
+    """simple_update of Muscle (src/Operations/simple_update.jl:35-82): contract
+    A and B over the bond, then with the gate G over the physical labels,
+    rename G's output labels back, thin SVD with the bond as the new label,
+    truncate to maxdim, normalise, absorb. absorb: None, "u", "v" or
+    "equally". Returns (U, s, Vt) or (U, Vt), each an (array, labels) pair."""
+    ia, ib, ig = list(ia), list(ib), list(ig)
+    l1 = setdiff(union(ia, ib), [bond])
+    t1 = contract(a, ia, b, ib, l1)
+    l2 = setdiff(union(l1, ig), [phys_a, phys_b])
+    theta = contract(t1, l1, g, ig, l2)
+    l2 = [phys_a if i == g_a else phys_b if i == g_b else i for i in l2]
+    inds_u, inds_v = setdiff(ia, [bond]), setdiff(ib, [bond])
+    U, s, Vt = tensor_svd_thin(theta, l2, inds_u, inds_v)
+    if maxdim is not None:
+        k = min(maxdim, s.shape[0])
+        U, s, Vt = U[..., :k], s[:k], Vt[..., :k]
+    if normalize:
+        s = s / np.linalg.norm(s)
+    lu, lv = inds_u + [bond], inds_v + [bond]
+    if absorb is None:
+        return (U, lu), (s, [bond]), (Vt, lv)
+    if absorb == "u":
+        U = U * s
+    elif absorb == "v":
+        Vt = Vt * s
+    elif absorb == "equally":
+        U, Vt = U * np.sqrt(s), Vt * np.sqrt(s)
+    return (np.array(U, order="F"), lu), (np.array(Vt, order="F"), lv)
 
 
 def exact_entries(a, ia, b, ib, ic, positions):

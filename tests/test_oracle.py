@@ -137,3 +137,47 @@ def test_generators_are_seeded():
         (pa, pia), (pb, pib), pic, tries = wl.peps_instance(100 + s)
         n = pa.size + pb.size + int(np.prod([dict(zip(pia + pib, pa.shape + pb.shape))[i] for i in pic]))
         assert n <= wl.PEPS_CAP
+
+
+def _su_case(op):
+    """The reference's simple_update test set-up (test/unit/operations/simple_update.jl:5-30):
+    an MPS of |00> + |01> + |10> + |11> (identity site tensors) and a two-site gate."""
+    I2 = np.eye(2)
+    g = np.array(op, dtype=float).reshape(2, 2, 2, 2, order="F")
+    return I2, ["s1", "b"], I2, ["s2", "b"], g, ["s1", "s2", "g1", "g2"]
+
+
+_OP_ID = np.eye(4)
+_OP_CX = [[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]]
+
+
+def _su(op, **kw):
+    a, ia, b, ib, g, ig = _su_case(op)
+    return ref.simple_update(a, ia, "s1", b, ib, "s2", "b", g, ig, "g1", "g2", **kw)
+
+
+def test_simple_update_restatement_matches_reference_asserts():
+    """The known answers of test/unit/operations/simple_update.jl:32-172."""
+    (U, lu), (s, ls), (V, lv) = _su(_OP_ID)  # apply identity
+    assert lu == ["s1", "b"] and lv == ["s2", "b"] and ls == ["b"]
+    assert np.allclose(U, np.eye(2)) and np.allclose(V, np.eye(2)) and np.array_equal(s, [1.0, 1.0])
+    (U, _), (s, _), (V, _) = _su(_OP_CX)  # apply cx
+    assert np.allclose(U, np.eye(2)) and np.allclose(V, np.array([[1, -1], [1, 1]]) / np.sqrt(2))
+    assert np.allclose(s, [np.sqrt(2), 0.0])
+    psi = ref.contract(U * s, ["s1", "b"], V, ["s2", "b"], ["s1", "s2"])
+    assert np.isclose(np.vdot(psi, psi).real, 2.0)
+    (U, _), (s, _), (V, _) = _su(_OP_ID, normalize=True)
+    assert np.allclose(s, [1 / np.sqrt(2)] * 2)
+    (U, _), (s, _), (V, _) = _su(_OP_CX, normalize=True)
+    assert np.allclose(s, [1.0, 0.0])
+    (U, _), (s, _), (V, _) = _su(_OP_ID, maxdim=1)
+    assert U.shape == (2, 1) and np.allclose(U, np.eye(2)[:, :1]) and np.allclose(s, [1.0])
+    (U, _), (s, _), (V, _) = _su(_OP_CX, maxdim=1)
+    assert np.allclose(V, np.ones((2, 1)) / np.sqrt(2)) and np.allclose(s, [np.sqrt(2)])
+    nrm = np.linalg.norm(ref.contract(np.eye(2), ["s1", "b"], np.eye(2), ["s2", "b"], ["s1", "s2"]))
+    (U, _), (V, _) = _su(_OP_ID, absorb="u")
+    assert np.isclose(np.linalg.norm(U), nrm)
+    (U, _), (V, _) = _su(_OP_ID, absorb="v")
+    assert np.isclose(np.linalg.norm(V), nrm)
+    (U, _), (V, _) = _su(_OP_ID, absorb="equally")
+    assert np.allclose(U, np.eye(2)) and np.allclose(V, np.eye(2))
