@@ -582,12 +582,23 @@ __device__ __forceinline__ int64_t oz_fixed(double x, int e) {
     else Q = 0;
     return (b >> 63) ? -Q : Q;
 }
-// The next signed digit of Q at weight 2^shift, rounded to nearest, taken out
-// of Q (the digits are produced most significant first).
-__device__ __forceinline__ int oz_take_digit(int64_t &Q, int shift) {
-    const int64_t dig = (Q + ((int64_t)1 << (shift - 1))) >> shift;
-    Q -= dig << shift;
-    return (int)dig;
+// Signed digits of Q, most significant first, rounded to nearest (balanced):
+// with B = half a unit of the last digit plus 2^(W-1) at every digit position
+// after the first, digit s >= 1 is the W-bit window of Q + B at its position
+// minus 2^(W-1), and the leading digit is everything above its position
+// (signed). |d_0| <= 2^W, |d_s| <= 2^(W-1), and the remainder below the last
+// digit lies in [-1/2, 1/2) units of it: the rounding of taking the digits
+// one at a time, with one 64-bit add for all of them instead of an add, a
+// shift and a subtract per digit.
+__device__ __forceinline__ int64_t oz_digit_bias(int S, int W) {
+    int64_t b = (int64_t)1 << (62 - W * S - 1);
+    for (int s = 1; s < S; ++s) b += (int64_t)1 << (62 - W * (s + 1) + W - 1);
+    return b;
+}
+__device__ __forceinline__ int oz_digit(int64_t Qb, int s, int W) {
+    const int sh = 62 - W * (s + 1);
+    if (s == 0) return (int)(Qb >> sh);
+    return (int)(((uint64_t)Qb >> sh) & ((1u << W) - 1u)) - (1 << (W - 1));
 }
 
 // Three bf16 pieces of a float: x = hi + mid + lo (to ~2^-24 relative).
@@ -696,14 +707,12 @@ __device__ __forceinline__ void oz_slice_tile(const T *__restrict__ X, const OpG
 #pragma unroll
                 for (int s = 0; s < 3; ++s) o[s * plane] = pack2(p0[s], p1[s]);
             } else {
-                int64_t q0 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx]), e);
-                int64_t q1 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx + 1]), e);
+                const int64_t bias = oz_digit_bias(S, W);
+                const int64_t q0 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx]), e) + bias;
+                const int64_t q1 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx + 1]), e) + bias;
 #pragma unroll 1
-                for (int s = 0; s < S; ++s, o += plane) {
-                    const int shift = 62 - W * (s + 1);
-                    const int d0 = oz_take_digit(q0, shift), d1 = oz_take_digit(q1, shift);
-                    *o = pack2(bf16_bits_of_int(d0), bf16_bits_of_int(d1));
-                }
+                for (int s = 0; s < S; ++s, o += plane)
+                    *o = pack2(bf16_bits_of_int(oz_digit(q0, s, W)), bf16_bits_of_int(oz_digit(q1, s, W)));
             }
         } else {
             int64_t word = k0 + tx;
@@ -726,12 +735,12 @@ __device__ __forceinline__ void oz_slice_tile(const T *__restrict__ X, const OpG
                     }
                 }
             } else {
-                int64_t qr = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][tx]), e);
-                int64_t qi = oz_fixed(bad ? 0.0 : (double)OzIn<T>::im(sm.tile[r][tx]), e);
+                const int64_t bias = oz_digit_bias(S, W);
+                const int64_t qr = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][tx]), e) + bias;
+                const int64_t qi = oz_fixed(bad ? 0.0 : (double)OzIn<T>::im(sm.tile[r][tx]), e) + bias;
 #pragma unroll 1
                 for (int s = 0; s < S; ++s, o += plane) {
-                    const int shift = 62 - W * (s + 1);
-                    const int dr = oz_take_digit(qr, shift), di = oz_take_digit(qi, shift);
+                    const int dr = oz_digit(qr, s, W), di = oz_digit(qi, s, W);
                     const uint32_t br = bf16_bits_of_int(dr), bi = bf16_bits_of_int(di);
                     if (MODE == MODE_CA) {
                         *o = pack2(br, bi);

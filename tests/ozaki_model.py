@@ -34,13 +34,23 @@ def row_exponents(x: np.ndarray) -> np.ndarray:
 
 
 def _digits(v: np.ndarray, S: int) -> list:
+    """Balanced digits as the slicer forms them: Q + B with B = half a unit of
+    the last digit plus 2^(W-1) at every digit position after the first;
+    digit s >= 1 is the W-bit window minus 2^(W-1), the leading digit all the
+    bits above its position."""
     W = digit_bits(S)
     Q = np.trunc(np.ldexp(v, 62)).astype(np.int64)
+    B = np.int64(1) << np.int64(62 - W * S - 1)
+    for s in range(1, S):
+        B += np.int64(1) << np.int64(62 - W * (s + 1) + W - 1)
+    Qb = Q + B
     out = []
     for s in range(S):
-        sh = 62 - W * (s + 1)
-        d = (Q + (np.int64(1) << (sh - 1))) >> sh
-        Q = Q - (d << sh)
+        sh = np.int64(62 - W * (s + 1))
+        if s == 0:
+            d = Qb >> sh
+        else:
+            d = ((Qb >> sh) & np.int64((1 << W) - 1)) - np.int64(1 << (W - 1))
         out.append(d.astype(np.float64))
     return out
 
