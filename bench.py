@@ -58,11 +58,13 @@ def parse():
     ap.add_argument("--native-steps", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "peps", "serve", "config2", "kernel", "permute", "hadamard", "unary", "fp64"],
+                    choices=["precision", "peps", "serve", "config2", "kernel", "permute", "hadamard", "unary", "fp64",
+                             "blocks"],
                     help="precision: the headline line; peps / serve: batching and serving forms; config2: "
                          "plain shapes that permute; kernel / permute: one contraction of the precision "
                          "workload at --n / the permutation of A(a,b,c,d,e) with e = --perm-e (profiling cases); "
-                         "hadamard / unary: broadcast product / partial sums of a 4.3 GB array")
+                         "hadamard / unary: broadcast product / partial sums of a 4.3 GB array; blocks: the "
+                         "precision workload at --n/2 contracted whole and block by block")
     ap.add_argument("--form", default="ozaki", help="form of --workload kernel")
     ap.add_argument("--band", type=int, default=0, help="rasterisation band of --workload kernel (0: default)")
     ap.add_argument("--perm-e", type=int, default=32, help="extent of label e in --workload permute")
@@ -638,6 +640,49 @@ def config2_bench(dev, steps=3):
     return res
 
 
+def blocks_bench(dev, n=4096, steps=3, warmup=1):
+    """The precision workload at M = N = n (K = 8192) contracted whole and
+    block by block (block_einsum: every block pair in one group, partial
+    products of contracted-label blocks summed by the unary kernel), TFLOP/s
+    of the whole contraction's flops, and the block result's distance from
+    the whole one."""
+    import torch
+
+    import muscle_gb300 as m
+    from muscle_gb300 import workloads as wl
+
+    (a, ia), (b, ib), ic = wl.gen_config3(seed=0, n=n)
+    A = m.Tensor(torch.from_numpy(a).to(dev), ia)
+    B = m.Tensor(torch.from_numpy(b).to(dev), ib)
+    del a, b
+    k1 = A.data.shape[ia.index("k1")]  # contracted labels k1, k2 (K = k1 k2)
+    splits = {"whole": {}, "K in 4": {"k1": k1 // 4}, "C in 2x2": {"i": n // 2, "j": n // 2},
+              "C in 2x2, K in 2": {"i": n // 2, "j": n // 2, "k1": k1 // 2}}
+    res, whole = {}, None
+    for name, bs in splits.items():
+        bc = m.BlockContraction(A, B, bs, out=ic)
+        for _ in range(warmup):
+            bc.execute()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            bc.execute()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        if whole is None:
+            whole = bc.c.data.clone()
+            err = 0.0
+        else:
+            err = float(torch.linalg.norm(bc.c.data - whole) / torch.linalg.norm(whole))
+        res[name] = {"ms": ms, "tflops": bc.flops / (ms / 1e3) / 1e12, "members": len(bc.group.items),
+                     "reductions": len(bc.reductions), "rel_diff_vs_whole": err}
+        del bc
+        torch.cuda.empty_cache()
+    return {"M": n, "N": n, "K": k1 * A.data.shape[ia.index("k2")], "dtype": "c64", "splits": res}
+
+
 def kernel_case(dev, n, form, slices, steps, warmup, band=0):
     """One contraction of the precision workload at M = N = n (K = 8192),
     launched warmup + steps times; phase timing from the plan."""
@@ -849,6 +894,9 @@ def main():
         elif args.workload == "hadamard":
             res = hadamard_case(dev, args.steps, args.warmup)
             metric = "hadamard (broadcast product) GB/s"
+        elif args.workload == "blocks":
+            res = blocks_bench(dev, args.n // 2)
+            metric = "block-partitioned contraction TFLOP/s against the whole contraction"
         else:
             res = serve_bench(dev, [1000, 3000, 10000, 30000, 100000], args.serve_seconds, n_requests=args.serve_pool)
             metric = "served contractions/s with p50/p99 ms (Poisson arrivals)"
@@ -1061,6 +1109,9 @@ def main():
     # batching form: a PEPS group of 1024 instances (the full one is --workload peps)
     peps = peps_bench(dev, 1024, quick=True, check=8)
     torch.cuda.empty_cache()
+    # block-partitioned form of the same workload at half the output extents
+    blocks = blocks_bench(dev, n // 2)
+    torch.cuda.empty_cache()
 
     # served mixed-size stream (short sweep; the full one is --workload serve)
     del cset, a_f, b_f
@@ -1108,6 +1159,7 @@ def main():
                          for k in ("c64", "c32")} | {"instances": peps["instances"],
                                                      "redraws_per_instance": peps["redraws_per_instance"],
                                                      "cap_elements": peps["cap_elements"]},
+            "blocks": blocks,
             "gpu_launches": launches_per_step * args.steps,
             "device_status": status,
             "clocks": clk.summary(),

@@ -42,6 +42,7 @@ from .ops import (
     unary_einsum_,
     unary_plan,
 )
+from .blocks import BlockContraction, BlockPlan, block_einsum
 from .grouped import Group, batched_contract
 from .serve import Request, Server
 from .tensor import (

@@ -10,7 +10,8 @@ and src/Operations/hadamard.jl:4-5 (none is replaced); the methods `ccall`
 into `libmuscle_gb300.so` (C ABI in include/muscle_gb300.h).
 `with_backend(f, BackendGB300(...))` selects a form explicitly. `Group` runs
 many independent contractions (a PEPS sweep's site pairs) as a few batched
-launches on one stream. `Server` is the serving loop: contractions submitted
+launches on one stream; `block_einsum` splits one contraction into blocks
+and runs them as such a group. `Server` is the serving loop: contractions submitted
 as they arrive, admitted against a device-memory budget and batched onto
 several streams.
 """
@@ -20,7 +21,7 @@ using CUDA
 using Muscle
 using Muscle: Backend, DomainCUDA, Index, Tensor, inds
 
-export BackendGB300, Server, submit!, Group, execute!
+export BackendGB300, Server, submit!, Group, execute!, block_einsum
 
 const libmgb = get(ENV, "MUSCLE_GB300_LIB", joinpath(@__DIR__, "..", "lib", "libmuscle_gb300.so"))
 
@@ -31,7 +32,8 @@ const FORMS = Dict(:auto => Cint(0), :plain => Cint(1), :ozaki => Cint(2), :bf16
 
 `form`: `:auto` (Ozaki emulation for Float64/ComplexF64 results, BF16x3 for
 Float32/ComplexF32), `:plain` (native FP64 DMMA / FP32 FFMA), `:ozaki`,
-`:bf16x3`. `slices`: Ozaki slice count (3..8; 0 means 7).
+`:bf16x3`. `slices`: Ozaki slice count (3..8; 0: chosen on the device per
+call, the fewest slices whose error estimate meets a 1e-13 relative target).
 """
 struct BackendGB300 <: Backend
     form::Cint
@@ -318,6 +320,74 @@ function set_bands!(g::Group, bands::AbstractVector{<:Integer})
     length(bands) == length(g.items) || throw(ArgumentError("one band per member"))
     check(ccall((:mgb_group_set_tiles, libmgb), Cint, (Ptr{Cvoid}, Ptr{Cint}), g.handle, Cint.(bands)))
     return g
+end
+
+"""
+    block_einsum(a, b, blocksize; out=nothing, rank=0, world=1, backend=BackendGB300())
+
+Block-partitioned contraction, the decomposition of
+ext/MuscleDaggerExt/binary_einsum.jl:64-119 on device tensors: `blocksize`
+maps labels to block sizes (each must divide its extent; other labels are one
+block). Every block pair runs as a member of one `Group` (views, no copies);
+the partial products of an output block, one per block of the contracted
+labels, are stacked along one extra label and summed by `unary_einsum!` (the
+reference's `treereduce(AddComputeOp, ...)`). With `world > 1` only the output
+blocks of replica `rank` are written, into a zero output, dealt largest work
+first to the least loaded replica.
+"""
+function block_einsum(a::Tensor, b::Tensor, blocksize::AbstractDict; out=nothing, rank::Integer=0,
+                      world::Integer=1, backend::BackendGB300=BackendGB300())
+    ia, ib = collect(inds(a)), collect(inds(b))
+    ic = out === nothing ? setdiff(union(ia, ib), intersect(ia, ib)) : collect(out)
+    ext = Dict{Index,Int}()
+    for (labs, t) in ((ia, a), (ib, b)), (k, i) in enumerate(labs)
+        haskey(ext, i) && ext[i] != size(t, k) && throw(DimensionMismatch("label $i has different extents"))
+        ext[i] = size(t, k)
+    end
+    all(i -> haskey(ext, i), ic) || throw(ArgumentError("ic must be a subset of ia ∪ ib"))
+    all(i -> haskey(ext, i), keys(blocksize)) || throw(ArgumentError("block size of a label of neither operand"))
+    bs = Dict(i => get(blocksize, i, ext[i]) for i in keys(ext))
+    for (i, s) in bs
+        (s > 0 && ext[i] % s == 0) || throw(ArgumentError("block size $s of label $i must divide $(ext[i])"))
+    end
+    0 <= rank < world || throw(ArgumentError("rank out of range"))
+    nb(i) = ext[i] ÷ bs[i]
+    rng(labels, co) = Tuple(haskey(co, i) ? ((co[i] * bs[i] + 1):((co[i] + 1) * bs[i])) : Colon() for i in labels)
+    sums = setdiff(union(ia, ib), ic)
+    T = promote_type(eltype(a), eltype(b))
+    C = Tensor(world > 1 ? CUDA.zeros(T, (ext[i] for i in ic)...) : CuArray{T}(undef, (ext[i] for i in ic)...), ic)
+    # output blocks, equal work each: dealt round robin over the replicas
+    outs = vec(collect(Iterators.product((0:(nb(i) - 1) for i in ic)...)))
+    mine = [o for (k, o) in enumerate(outs) if (k - 1) % world == rank]
+    ksets = vec(collect(Iterators.product((0:(nb(i) - 1) for i in sums)...)))
+    items, reductions, part = Any[], Any[], Index(gensym(:block_part))
+    for o in mine
+        co = Dict(zip(ic, o))
+        cview = Tensor(view(parent(C), rng(ic, co)...), ic)
+        pairs = map(ksets) do kc
+            c2 = merge(co, Dict(zip(sums, kc)))
+            (Tensor(view(parent(a), rng(ia, c2)...), ia), Tensor(view(parent(b), rng(ib, c2)...), ib))
+        end
+        if length(pairs) == 1
+            push!(items, (cview, pairs[1]...))
+        else
+            P = CuArray{T}(undef, (bs[i] for i in ic)..., length(pairs))
+            for (k, (va, vb)) in enumerate(pairs)
+                push!(items, (Tensor(view(P, ntuple(_ -> Colon(), length(ic))..., k), ic), va, vb))
+            end
+            push!(reductions, (cview, Tensor(P, [ic; part])))
+        end
+    end
+    if !isempty(items)
+        g = Group(items; backend)
+        execute!(g)
+        for (y, x) in reductions
+            Muscle.unary_einsum!(backend, y, x)
+        end
+        CUDA.synchronize()
+        close(g)
+    end
+    return C
 end
 
 function Base.close(g::Group)
