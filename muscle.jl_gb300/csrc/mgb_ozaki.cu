@@ -282,11 +282,16 @@ __device__ __forceinline__ int bexp_of(float2 v) { return max(bexp((double)v.x),
 // 2^(2 d) as a float (0 below 2^-126)
 __device__ __forceinline__ float pow4f(int d) { return d >= -63 ? __int_as_float((127 + 2 * d) << 23) : 0.f; }
 
+// k per tile of the exponent scan: each thread issues eight loads before
+// the first reduction.
+constexpr int OZ_SCAN_KT = 64;
+
 struct ScaleSmem {
-    int64_t roff[32], koff[32];
+    int64_t roff[32], koff[OZ_SCAN_KT];
     int red[8][33];
-    int cmax[8][33];    // partials: per-warp column maxima
-    float csum[8][33];  // partials: per-warp column sums
+    int cmax[8][OZ_SCAN_KT + 1];    // partials: per-warp column maxima
+    float csum[8][OZ_SCAN_KT + 1];  // partials: per-warp column sums
+    int tmax[OZ_SCAN_KT];           // partials: column maxima over the tile
 };
 
 // |x|^2 4^-(t - 1023), from the exponent and the top of the mantissa, for an
@@ -303,77 +308,93 @@ __device__ __forceinline__ float sq_tile(double2 x, int t) { return sq_tile(x.x,
 __device__ __forceinline__ float sq_tile(float x, int t) { return sq_tile((double)x, t); }
 __device__ __forceinline__ float sq_tile(float2 x, int t) { return sq_tile((double)x.x, t) + sq_tile((double)x.y, t); }
 template <typename T>
-// `part` (nullable, adaptive plans): per 32-row tile and k, the tile's
-// largest exponent t and the sum of |x|^2 4^-(t - 1023) over its rows,
-// at part[(l * ceil(R / 32) + tile) * K + k].
+// One 32-row x 64-k tile. `part` (nullable, adaptive plans): per 32-row tile
+// and k, the tile's largest exponent t and the sum of |x|^2 4^-(t - 1023)
+// over its rows, at part[(l * ceil(R / 32) + tile) * K + k].
 __device__ __forceinline__ void oz_scale_tile(const T *__restrict__ X, const OpGeom &g, int32_t *exps,
                                               int32_t *emax, int2 *part, int64_t blk, int64_t l, ScaleSmem &sm) {
-    int64_t tiles_k = (g.K + 31) / 32;
+    constexpr int KT = OZ_SCAN_KT;
+    int64_t tiles_k = (g.K + KT - 1) / KT;
     int64_t tr = blk / tiles_k, tk = blk - tr * tiles_k;
-    int64_t r0 = tr * 32, k0 = tk * 32;
+    int64_t r0 = tr * 32, k0 = tk * KT;
     int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
     if (tid < 32) sm.roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
-    else if (tid < 64) sm.koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
+    else if (tid < 32 + KT) sm.koff[tid - 32] = (k0 + tid - 32 < g.K) ? group_offset(g.gk, g.t, k0 + tid - 32) : 0;
     const T *Xl = g.ptrs ? (const T *)g.ptrs[l] : X + group_offset(g.gl, g.t, l);
     __syncthreads();
     const int64_t R32 = (g.R + 31) / 32;
     int2 *pt = part ? part + (l * R32 + tr) * g.K + k0 : nullptr;  // this tile's partials
-    if (g.rows_fast) {  // lanes walk rows
+    if (g.rows_fast) {  // lanes walk rows; thread column kk = ty + 8 j
+        constexpr int NJ = KT / 8;
+        const bool rin = r0 + tx < g.R;
+        T v[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            memset(&v[j], 0, sizeof(T));
+            if (rin && k0 + ty + 8 * j < g.K) v[j] = __ldg(Xl + sm.roff[tx] + sm.koff[ty + 8 * j]);
+        }
         int e = 0;
-        int64_t r = r0 + tx;
-        for (int kk = ty; kk < 32; kk += 8) {
-            const bool in = r < g.R && k0 + kk < g.K;
-            T v;
-            int be = 0;
-            if (in) {
-                v = __ldg(Xl + sm.roff[tx] + sm.koff[kk]);
-                be = bexp_of(v);
-                e = max(e, be);
-            }
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int be = bexp_of(v[j]);  // zero-filled outside the operand: 0
+            e = max(e, be);
             if (pt) {
                 int t = be;
 #pragma unroll
                 for (int d = 16; d > 0; d >>= 1) t = max(t, __shfl_xor_sync(0xffffffffu, t, d));
-                float q = in ? sq_tile(v, t) : 0.f;
+                float q = sq_tile(v[j], t);
 #pragma unroll
                 for (int d = 16; d > 0; d >>= 1) q += __shfl_xor_sync(0xffffffffu, q, d);
-                if (tx == 0 && k0 + kk < g.K) pt[kk] = make_int2(t, __float_as_int(q));
+                if (tx == 0 && k0 + ty + 8 * j < g.K) pt[ty + 8 * j] = make_int2(t, __float_as_int(q));
             }
         }
         sm.red[ty][tx] = e;
-    } else {  // lanes walk k
-        T v[4];
-        int be4[4];
+    } else {  // lanes walk k: columns tx and tx + 32, rows ty + 8 j
+        T v[4][2];
+        int be[4][2];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                memset(&v[j][h], 0, sizeof(T));
+                if (r0 + ty + 8 * j < g.R && k0 + tx + 32 * h < g.K)
+                    v[j][h] = __ldg(Xl + sm.roff[ty + 8 * j] + sm.koff[tx + 32 * h]);
+            }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            int rr = ty + 8 * j;
-            be4[j] = 0;
-            if (r0 + rr < g.R && k0 + tx < g.K) {
-                v[j] = __ldg(Xl + sm.roff[rr] + sm.koff[tx]);
-                be4[j] = bexp_of(v[j]);
-            }
-            int e = be4[j];
+            be[j][0] = bexp_of(v[j][0]);
+            be[j][1] = bexp_of(v[j][1]);
+            int e = max(be[j][0], be[j][1]);
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, d));
-            if (tx == 0) sm.red[j][rr] = e;  // rows rr = ty + 8 j are distinct per (ty, j)
+            if (tx == 0) sm.red[j][ty + 8 * j] = e;  // rows ty + 8 j are distinct per (ty, j)
         }
         if (pt) {
-            sm.cmax[ty][tx] = max(max(be4[0], be4[1]), max(be4[2], be4[3]));
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                sm.cmax[ty][tx + 32 * h] = max(max(be[0][h], be[1][h]), max(be[2][h], be[3][h]));
             __syncthreads();
-            int t = 0;
 #pragma unroll
-            for (int y = 0; y < 8; ++y) t = max(t, sm.cmax[y][tx]);
-            float q = 0.f;
+            for (int h = 0; h < 2; ++h) {
+                int t = 0;
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-                if (be4[j] > 0) q += sq_tile(v[j], t);
-            sm.csum[ty][tx] = q;
+                for (int y = 0; y < 8; ++y) t = max(t, sm.cmax[y][tx + 32 * h]);
+                float q = 0.f;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (be[j][h] > 0) q += sq_tile(v[j][h], t);
+                sm.csum[ty][tx + 32 * h] = q;
+                if (ty == 0) sm.tmax[tx + 32 * h] = t;
+            }
             __syncthreads();
-            if (ty == 0 && k0 + tx < g.K) {
-                float s2 = 0.f;
+            if (ty < 2) {
+                const int c = tx + 32 * ty;
+                if (k0 + c < g.K) {
+                    float s2 = 0.f;
 #pragma unroll
-                for (int y = 0; y < 8; ++y) s2 += sm.csum[y][tx];
-                pt[tx] = make_int2(t, __float_as_int(s2));
+                    for (int y = 0; y < 8; ++y) s2 += sm.csum[y][c];
+                    pt[c] = make_int2(sm.tmax[c], __float_as_int(s2));
+                }
             }
         }
     }
@@ -427,8 +448,12 @@ struct OzStats {
     int32_t emax[2];    // largest biased exponent of A and B
     float est[9];       // estimated error per candidate slice count
     int32_t pad[3];
+    // sums over k and batch entries (cleared with the header every call):
+    // P_A sum q_B + P_B sum q_A, sum q_A q_B, K P_A P_B
+    double acc[3];
+    double pad2;
 };
-static_assert(sizeof(OzStats) == 64, "stats header");
+static_assert(sizeof(OzStats) == 96, "stats header");
 
 
 
@@ -483,46 +508,59 @@ __global__ void __launch_bounds__(256) k_oz_stat(const int2 *__restrict__ part, 
 }
 __host__ __device__ inline int64_t oz_stat_blocks(int64_t R, int64_t K) { return (K + 255) / 256 + (R + 255) / 256; }
 
-// One block: the error estimate of every candidate slice count (bit S of
-// `cand`) and the choice, the smallest count within `tol`, else 0 (plain).
-__device__ __forceinline__ void oz_choose_body(OzStats *st, const float *__restrict__ qa, const float *__restrict__ qb,
-                                               const float *__restrict__ pa, const float *__restrict__ pb, int64_t K,
-                                               int64_t L, uint32_t cand, double tol, double margin, int cx) {
-    __shared__ double red[3][32];
-    double trunc = 0.0, drop = 0.0, den = 0.0;
-    for (int64_t l = 0; l < L; ++l) {
-        double sa = 0.0, sb = 0.0, d = 0.0;
-        for (int64_t k = threadIdx.x; k < K; k += blockDim.x) {
-            const double x = qa[l * K + k], y = qb[l * K + k];
-            sa += x;
-            sb += y;
-            d += x * y;
-        }
-        const double Pa = pa[l], Pb = pb[l];
-        trunc += Pa * sb + Pb * sa;
-        den += d;
-        if (threadIdx.x == 0) drop += (double)K * Pa * Pb;
+// The sums behind the estimate, spread over the GPU: block b of batch entry
+// l (flattened as l * blocks + b) covers OZ_EST_K values of k and adds its
+// part of P_A sum q_B + P_B sum q_A and of sum q_A q_B into the header in
+// double; the entry's first block adds K P_A P_B.
+constexpr int OZ_EST_K = 2048;
+__host__ __device__ inline int64_t oz_est_blocks(int64_t K) { return (K + OZ_EST_K - 1) / OZ_EST_K; }
+__device__ __forceinline__ void oz_est_block(OzStats *st, const float *__restrict__ qa, const float *__restrict__ qb,
+                                             const float *__restrict__ pa, const float *__restrict__ pb, int64_t K,
+                                             int64_t blk, int64_t l, double (&red)[2][8]) {
+    double sa = 0.0, sb = 0.0, d = 0.0;
+    const int64_t k1 = min(K, (blk + 1) * OZ_EST_K);
+    for (int64_t k = blk * OZ_EST_K + threadIdx.x; k < k1; k += blockDim.x) {
+        const float x = __ldg(qa + l * K + k), y = __ldg(qb + l * K + k);
+        sa += x;
+        sb += y;
+        d += (double)x * y;
     }
-    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+    const double Pa = pa[l], Pb = pb[l];
+    double tr = Pa * sb + Pb * sa;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        trunc += __shfl_xor_sync(0xffffffffu, trunc, o);
-        drop += __shfl_xor_sync(0xffffffffu, drop, o);
-        den += __shfl_xor_sync(0xffffffffu, den, o);
+        tr += __shfl_xor_sync(0xffffffffu, tr, o);
+        d += __shfl_xor_sync(0xffffffffu, d, o);
     }
+    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
     if (lane == 0) {
-        red[0][w] = trunc;
-        red[1][w] = drop;
-        red[2][w] = den;
+        red[0][w] = tr;
+        red[1][w] = d;
     }
     __syncthreads();
-    if (threadIdx.x != 0) return;
-    trunc = drop = den = 0.0;
-    for (int i = 0; i < (int)(blockDim.x + 31) / 32; ++i) {
-        trunc += red[0][i];
-        drop += red[1][i];
-        den += red[2][i];
+    if (threadIdx.x == 0) {
+        tr = d = 0.0;
+        for (int i = 0; i < (int)blockDim.x / 32; ++i) {
+            tr += red[0][i];
+            d += red[1][i];
+        }
+        if (tr != 0.0) atomicAdd(&st->acc[0], tr);
+        if (d != 0.0) atomicAdd(&st->acc[1], d);
+        if (blk == 0 && Pa * Pb != 0.0) atomicAdd(&st->acc[2], (double)K * Pa * Pb);
     }
+}
+__global__ void __launch_bounds__(256) k_oz_est(OzStats *st, const float *__restrict__ qa, const float *__restrict__ qb,
+                                                const float *__restrict__ pa, const float *__restrict__ pb, int64_t K) {
+    __shared__ double red[2][8];
+    const int64_t nb = oz_est_blocks(K), l = blockIdx.x / nb;
+    oz_est_block(st, qa, qb, pa, pb, K, blockIdx.x - l * nb, l, red);
+}
+
+// One thread: the error estimate of every candidate slice count (bit S of
+// `cand`) from the sums, and the choice, the smallest count within `tol`,
+// else 0 (plain).
+__device__ __forceinline__ void oz_choose_final(OzStats *st, uint32_t cand, double tol, double margin, int cx) {
+    const double trunc = st->acc[0], den = st->acc[1], drop = st->acc[2];
     const double f1 = cx ? 2.0 : 1.0, f2 = cx ? 4.0 : 1.0;
     int sel = 0;
     for (int S = 8; S >= 1; --S) {
@@ -541,11 +579,8 @@ __device__ __forceinline__ void oz_choose_body(OzStats *st, const float *__restr
     st->est[0] = 0.f;
     st->sel = sel;
 }
-__global__ void __launch_bounds__(1024) k_oz_choose(OzStats *st, const float *__restrict__ qa,
-                                                    const float *__restrict__ qb, const float *__restrict__ pa,
-                                                    const float *__restrict__ pb, int64_t K, int64_t L,
-                                                    uint32_t cand, double tol, double margin, int cx) {
-    oz_choose_body(st, qa, qb, pa, pb, K, L, cand, tol, margin, cx);
+__global__ void k_oz_choose(OzStats *st, uint32_t cand, double tol, double margin, int cx) {
+    if (threadIdx.x == 0) oz_choose_final(st, cand, tol, margin, cx);
 }
 
 // =============================================================================
@@ -590,15 +625,41 @@ __device__ __forceinline__ int64_t oz_fixed(double x, int e) {
 // digit lies in [-1/2, 1/2) units of it: the rounding of taking the digits
 // one at a time, with one 64-bit add for all of them instead of an add, a
 // shift and a subtract per digit.
-__device__ __forceinline__ int64_t oz_digit_bias(int S, int W) {
+__host__ __device__ constexpr int64_t oz_digit_bias(int S, int W) {
     int64_t b = (int64_t)1 << (62 - W * S - 1);
     for (int s = 1; s < S; ++s) b += (int64_t)1 << (62 - W * (s + 1) + W - 1);
     return b;
 }
-__device__ __forceinline__ int oz_digit(int64_t Qb, int s, int W) {
-    const int sh = 62 - W * (s + 1);
-    if (s == 0) return (int)(Qb >> sh);
-    return (int)(((uint64_t)Qb >> sh) & ((1u << W) - 1u)) - (1 << (W - 1));
+// Digit s of a biased value Qb (Q + oz_digit_bias) as an exact float. The
+// leading digit (signed, |d| <= 2^W) goes through 1.5 * 2^23 + d; a later
+// digit's W-bit window u becomes the mantissa of 2^23 + u, from which
+// 2^23 + 2^(W-1) is subtracted: a funnel shift, a mask-and-or and one add,
+// with no integer-to-float conversion. NEG gives -d (+0 for d = 0, as d).
+template <int W, int s, bool NEG = false>
+__device__ __forceinline__ float oz_digit_f(int64_t Qb) {
+    constexpr int sh = 62 - W * (s + 1);
+    if constexpr (s == 0) {
+        const float m = __int_as_float(0x4B400000 + (int)(Qb >> sh));
+        return NEG ? 12582912.0f - m : m - 12582912.0f;
+    } else {
+        constexpr float c = 8388608.0f + (float)(1 << (W - 1));
+        const float m = __uint_as_float(0x4B000000u | ((uint32_t)((uint64_t)Qb >> sh) & ((1u << W) - 1u)));
+        return NEG ? c - m : m - c;
+    }
+}
+// Two floats that bf16 holds exactly (the digits) as one packed word, `lo`
+// in the low half: one conversion instruction.
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+// f(integral_constant<int, s>) for s = 0 .. N-1, unrolled at compile time.
+template <int N, int s = 0, typename F>
+__device__ __forceinline__ void oz_static_for(F &&f) {
+    if constexpr (s < N) {
+        f(std::integral_constant<int, s>{});
+        oz_static_for<N, s + 1>(f);
+    }
 }
 
 // Three bf16 pieces of a float: x = hi + mid + lo (to ~2^-24 relative).
@@ -647,19 +708,118 @@ struct SliceSmem {
     int64_t roff[32], koff[KT];
     int rexp[32];
 };
+// k per slicer tile: eight loads per thread before the barrier
+constexpr int OZ_SLICE_KT = 64;
 template <typename T, int MODE>
-using SliceSmemOf = SliceSmem<T, MODE == MODE_REAL ? 64 : 32>;
+using SliceSmemOf = SliceSmem<T, OZ_SLICE_KT>;
 
+// BF16x3: three bf16 pieces per float, one thread per (row, k word).
+template <typename T, int MODE>
+__device__ __forceinline__ void oz_write_pieces(const SliceSmemOf<T, MODE> &sm, const OpGeom &g, uint32_t *outl,
+                                                int64_t plane, int64_t kw, int64_t r0, int64_t k0) {
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    for (int j = 0; j < 4; ++j) {
+        const int r = ty + 8 * j;
+        const int64_t row = r0 + r;
+        if (row >= g.R) continue;
+        if constexpr (MODE == MODE_REAL) {
+            const int64_t word = k0 / 2 + tx;
+            if (word >= kw) continue;
+            uint32_t *o = outl + row * kw + word;
+            uint32_t p0[8], p1[8];
+            bf3_pieces((float)OzIn<T>::re(sm.tile[r][2 * tx]), p0);
+            bf3_pieces((float)OzIn<T>::re(sm.tile[r][2 * tx + 1]), p1);
+#pragma unroll
+            for (int s = 0; s < 3; ++s) o[s * plane] = pack2(p0[s], p1[s]);
+        } else {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int kk = tx + 32 * h;
+                const int64_t word = k0 + kk;
+                if (word >= kw) continue;
+                // MODE_CA: row r; MODE_CB: rows 2r (re, -im) and 2r + 1 (im, re)
+                uint32_t *o = outl + (MODE == MODE_CB ? 2 * row : row) * kw + word;
+                uint32_t pr[8], pi[8], pn[8];
+                bf3_pieces((float)OzIn<T>::re(sm.tile[r][kk]), pr);
+                bf3_pieces((float)OzIn<T>::im(sm.tile[r][kk]), pi);
+                bf3_pieces(-(float)OzIn<T>::im(sm.tile[r][kk]), pn);
+#pragma unroll
+                for (int s = 0; s < 3; ++s) {
+                    if (MODE == MODE_CA) {
+                        o[s * plane] = pack2(pr[s], pi[s]);
+                    } else {
+                        o[s * plane] = pack2(pr[s], pn[s]);
+                        o[s * plane + kw] = pack2(pi[s], pr[s]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Ozaki digits with the slice count fixed at compile time: every digit plane
+// is written as soon as it is known, from two biased fixed-point values per
+// thread.
+template <int S, typename T, int MODE>
+__device__ __forceinline__ void oz_write_digits(const SliceSmemOf<T, MODE> &sm, const OpGeom &g, uint32_t *outl,
+                                                int64_t plane, int64_t kw, int64_t r0, int64_t k0) {
+    constexpr int W = oz_digit_bits(S);
+    constexpr int64_t bias = oz_digit_bias(S, W);
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    for (int j = 0; j < 4; ++j) {
+        const int r = ty + 8 * j;
+        const int64_t row = r0 + r;
+        if (row >= g.R) continue;
+        int e = sm.rexp[r];
+        const bool bad = e == 0x7FFFFFFF;
+        if (bad) e = 0;
+        if constexpr (MODE == MODE_REAL) {
+            const int64_t word = k0 / 2 + tx;
+            if (word >= kw) continue;
+            uint32_t *o = outl + row * kw + word;
+            const int64_t q0 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx]), e) + bias;
+            const int64_t q1 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx + 1]), e) + bias;
+            oz_static_for<S>([&](auto sc) {
+                constexpr int s = decltype(sc)::value;
+                o[s * plane] = pack_bf16x2(oz_digit_f<W, s>(q0), oz_digit_f<W, s>(q1));
+            });
+        } else {
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+                const int kk = tx + 32 * h;
+                const int64_t word = k0 + kk;
+                if (word >= kw) continue;
+                uint32_t *o = outl + (MODE == MODE_CB ? 2 * row : row) * kw + word;
+                const int64_t qr = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][kk]), e) + bias;
+                const int64_t qi = oz_fixed(bad ? 0.0 : (double)OzIn<T>::im(sm.tile[r][kk]), e) + bias;
+                oz_static_for<S>([&](auto sc) {
+                    constexpr int s = decltype(sc)::value;
+                    const float dr = oz_digit_f<W, s>(qr), di = oz_digit_f<W, s>(qi);
+                    if constexpr (MODE == MODE_CA) {
+                        o[s * plane] = pack_bf16x2(dr, di);
+                    } else {
+                        o[s * plane] = pack_bf16x2(dr, oz_digit_f<W, s, true>(qi));
+                        o[s * plane + kw] = pack_bf16x2(di, dr);
+                    }
+                });
+            }
+        }
+    }
+}
+
+// One 32-row tile of an operand: staged through shared memory (coalesced
+// reads whichever mode is contiguous), then written as digit (or piece)
+// planes [L][S][rows_e][kw] with K contiguous.
 template <typename T, int MODE, bool BF3>
 __device__ __forceinline__ void oz_slice_tile(const T *__restrict__ X, const OpGeom &g,
-                                              const int32_t *__restrict__ exps, int S, int W,
+                                              const int32_t *__restrict__ exps, int S,
                                               uint32_t *__restrict__ out, int64_t rows_e, int64_t kw, int64_t blk,
                                               int64_t l, SliceSmemOf<T, MODE> &sm) {
-    constexpr int KT = MODE == MODE_REAL ? 64 : 32;  // k per tile
+    constexpr int KT = OZ_SLICE_KT;
     int64_t tiles_k = (g.K + KT - 1) / KT;
     int64_t tr = blk / tiles_k, tk = blk - tr * tiles_k;
     int64_t r0 = tr * 32, k0 = tk * KT;
-    int tid = threadIdx.x, tx = tid % 32, ty = tid / 32;
+    int tid = threadIdx.x;
     if (tid < 32) {
         sm.roff[tid] = (r0 + tid < g.R) ? group_offset(g.gr, g.t, r0 + tid) : 0;
         if (!BF3) {
@@ -687,69 +847,17 @@ __device__ __forceinline__ void oz_slice_tile(const T *__restrict__ X, const OpG
     __syncthreads();
     const int64_t plane = rows_e * kw;
     uint32_t *outl = out + l * (int64_t)S * plane;
-    // Each digit (or piece) plane is written as soon as it is known, so a
-    // thread holds two fixed-point values rather than arrays of digits.
-    for (int j = 0; j < 4; ++j) {
-        int r = ty + 8 * j;
-        int64_t row = r0 + r;
-        if (row >= g.R) continue;
-        int e = BF3 ? 0 : sm.rexp[r];
-        bool bad = !BF3 && e == 0x7FFFFFFF;
-        if (bad) e = 0;
-        if (MODE == MODE_REAL) {
-            int64_t word = k0 / 2 + tx;
-            if (word >= kw) continue;
-            uint32_t *o = outl + row * kw + word;
-            if (BF3) {
-                uint32_t p0[8], p1[8];
-                bf3_pieces((float)OzIn<T>::re(sm.tile[r][2 * tx]), p0);
-                bf3_pieces((float)OzIn<T>::re(sm.tile[r][2 * tx + 1]), p1);
-#pragma unroll
-                for (int s = 0; s < 3; ++s) o[s * plane] = pack2(p0[s], p1[s]);
-            } else {
-                const int64_t bias = oz_digit_bias(S, W);
-                const int64_t q0 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx]), e) + bias;
-                const int64_t q1 = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][2 * tx + 1]), e) + bias;
-#pragma unroll 1
-                for (int s = 0; s < S; ++s, o += plane)
-                    *o = pack2(bf16_bits_of_int(oz_digit(q0, s, W)), bf16_bits_of_int(oz_digit(q1, s, W)));
-            }
-        } else {
-            int64_t word = k0 + tx;
-            if (word >= kw) continue;
-            // MODE_CA: row r; MODE_CB: rows 2r (re, -im) and 2r + 1 (im, re)
-            uint32_t *o = outl + (MODE == MODE_CB ? 2 * row : row) * kw + word;
-            if (BF3) {
-                uint32_t pr[8], pi[8], pn[8];
-                bf3_pieces((float)OzIn<T>::re(sm.tile[r][tx]), pr);
-                bf3_pieces((float)OzIn<T>::im(sm.tile[r][tx]), pi);
-                float nim = -(float)OzIn<T>::im(sm.tile[r][tx]);
-                bf3_pieces(nim, pn);
-#pragma unroll
-                for (int s = 0; s < 3; ++s) {
-                    if (MODE == MODE_CA) {
-                        o[s * plane] = pack2(pr[s], pi[s]);
-                    } else {
-                        o[s * plane] = pack2(pr[s], pn[s]);
-                        o[s * plane + kw] = pack2(pi[s], pr[s]);
-                    }
-                }
-            } else {
-                const int64_t bias = oz_digit_bias(S, W);
-                const int64_t qr = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][tx]), e) + bias;
-                const int64_t qi = oz_fixed(bad ? 0.0 : (double)OzIn<T>::im(sm.tile[r][tx]), e) + bias;
-#pragma unroll 1
-                for (int s = 0; s < S; ++s, o += plane) {
-                    const int dr = oz_digit(qr, s, W), di = oz_digit(qi, s, W);
-                    const uint32_t br = bf16_bits_of_int(dr), bi = bf16_bits_of_int(di);
-                    if (MODE == MODE_CA) {
-                        *o = pack2(br, bi);
-                    } else {
-                        o[0] = pack2(br, bf16_bits_of_int(-di));
-                        o[kw] = pack2(bi, br);
-                    }
-                }
-            }
+    if constexpr (BF3) {
+        oz_write_pieces<T, MODE>(sm, g, outl, plane, kw, r0, k0);
+    } else {
+        switch (S) {
+        case 3: oz_write_digits<3, T, MODE>(sm, g, outl, plane, kw, r0, k0); break;
+        case 4: oz_write_digits<4, T, MODE>(sm, g, outl, plane, kw, r0, k0); break;
+        case 5: oz_write_digits<5, T, MODE>(sm, g, outl, plane, kw, r0, k0); break;
+        case 6: oz_write_digits<6, T, MODE>(sm, g, outl, plane, kw, r0, k0); break;
+        case 7: oz_write_digits<7, T, MODE>(sm, g, outl, plane, kw, r0, k0); break;
+        case 8: oz_write_digits<8, T, MODE>(sm, g, outl, plane, kw, r0, k0); break;
+        default: break;  // plans hold 3..8
         }
     }
 }
@@ -757,17 +865,16 @@ __device__ __forceinline__ void oz_slice_tile(const T *__restrict__ X, const OpG
 // `sel` (nullable): the adaptive choice; the slice count is read from it and
 // the launch does nothing when it is 0 (plain).
 template <typename T, int MODE, bool BF3>
-__global__ void __launch_bounds__(256, 6) k_oz_slice(const T *__restrict__ X, OpGeom g,
-                                                  const int32_t *__restrict__ exps, int S, int W,
+__global__ void __launch_bounds__(256, 4) k_oz_slice(const T *__restrict__ X, OpGeom g,
+                                                  const int32_t *__restrict__ exps, int S,
                                                   uint32_t *__restrict__ out, int64_t rows_e,
                                                   int64_t kw, const int32_t *__restrict__ sel) {
     if (sel) {
         S = *sel;
         if (S == 0) return;
-        W = S <= 6 ? 8 : 7;
     }
     __shared__ SliceSmemOf<T, MODE> sm;
-    oz_slice_tile<T, MODE, BF3>(X, g, exps, S, W, out, rows_e, kw, blockIdx.x, blockIdx.y, sm);
+    oz_slice_tile<T, MODE, BF3>(X, g, exps, S, out, rows_e, kw, blockIdx.x, blockIdx.y, sm);
 }
 
 // =============================================================================
@@ -1481,15 +1588,14 @@ static int unit_row_fast(const ModeGroup &gr, const ModeGroup &gk, int t) {
 template <typename T, bool BF3>
 static int run_prepass(const OpGeom &g, int mode, const void *X, int32_t *exps, int S, uint32_t *out,
                        int64_t rows_e, int64_t kw, int64_t L, cudaStream_t s, const int32_t *sel = nullptr) {
-    int KT = mode == MODE_REAL ? 64 : 32;
-    int64_t tiles = ((g.R + 31) / 32) * ((g.K + KT - 1) / KT);
+    int64_t tiles = ((g.R + 31) / 32) * ((g.K + OZ_SLICE_KT - 1) / OZ_SLICE_KT);
     if (tiles > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the slicer grid");
     dim3 grid((unsigned)tiles, (unsigned)L);
     const T *x = (const T *)X;
     switch (mode) {
-    case MODE_REAL: k_oz_slice<T, MODE_REAL, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw, sel); break;
-    case MODE_CA: k_oz_slice<T, MODE_CA, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw, sel); break;
-    default: k_oz_slice<T, MODE_CB, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, oz_digit_bits(S), out, rows_e, kw, sel); break;
+    case MODE_REAL: k_oz_slice<T, MODE_REAL, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, out, rows_e, kw, sel); break;
+    case MODE_CA: k_oz_slice<T, MODE_CA, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, out, rows_e, kw, sel); break;
+    default: k_oz_slice<T, MODE_CB, BF3><<<grid, 256, 0, s>>>(x, g, exps, S, out, rows_e, kw, sel); break;
     }
     MGB_CUDA_CHECK(cudaGetLastError());
     return MGB_OK;
@@ -1498,7 +1604,7 @@ static int run_prepass(const OpGeom &g, int mode, const void *X, int32_t *exps, 
 template <typename T>
 static int run_scale(const OpGeom &g, const void *X, int32_t *exps, int64_t L, cudaStream_t s,
                      int32_t *emax = nullptr, int2 *part = nullptr) {
-    int64_t tiles = ((g.R + 31) / 32) * ((g.K + 31) / 32);
+    int64_t tiles = ((g.R + 31) / 32) * ((g.K + OZ_SCAN_KT - 1) / OZ_SCAN_KT);
     if (tiles > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the scale grid");
     dim3 grid((unsigned)tiles, (unsigned)L);
     k_oz_scale<T><<<grid, 256, 0, s>>>((const T *)X, g, exps, emax, part);
@@ -1572,8 +1678,11 @@ int ozaki_prepass(const ContractionPlan &p, const void *A, const void *B, void *
             // Fluctuations of a Frobenius norm over few outputs: a margin that
             // vanishes for large results.
             const double margin = 1.0 + 2.0 / std::sqrt((double)std::max<int64_t>(p.M * p.N * p.L, 1));
-            k_oz_choose<<<1, 1024, 0, s>>>(sa_.st, sa_.qa, sa_.qb, sa_.pa, sa_.pb, p.K, p.L, p.cand_mask, p.tol,
-                                           margin, cx ? 1 : 0);
+            const int64_t eb = oz_est_blocks(p.K) * p.L;
+            if (eb > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "operand too large for the estimate grid");
+            k_oz_est<<<(unsigned)eb, 256, 0, s>>>(sa_.st, sa_.qa, sa_.qb, sa_.pa, sa_.pb, p.K);
+            MGB_CUDA_CHECK(cudaGetLastError());
+            k_oz_choose<<<1, 32, 0, s>>>(sa_.st, p.cand_mask, p.tol, margin, cx ? 1 : 0);
             MGB_CUDA_CHECK(cudaGetLastError());
         }
         st = by_type(p.a.dtype, [&](auto tag) {
@@ -1805,26 +1914,26 @@ union PreSmem {
 };
 
 template <typename T, bool BF3>
-__device__ __forceinline__ void pre_slice_typed(const PreJob &J, int S, int W, int64_t blk, int64_t l, PreSmem &sm) {
+__device__ __forceinline__ void pre_slice_typed(const PreJob &J, int S, int64_t blk, int64_t l, PreSmem &sm) {
     const T *X = (const T *)J.X;
     switch (J.mode) {
     case MODE_REAL:
         if constexpr (!OzIn<T>::cx)
-            oz_slice_tile<T, MODE_REAL, BF3>(X, J.g, J.exps, S, W, J.out, J.rows_e, J.kw, blk, l,
+            oz_slice_tile<T, MODE_REAL, BF3>(X, J.g, J.exps, S, J.out, J.rows_e, J.kw, blk, l,
                                              *reinterpret_cast<SliceSmemOf<T, MODE_REAL> *>(&sm));
         break;
     case MODE_CA:
-        oz_slice_tile<T, MODE_CA, BF3>(X, J.g, J.exps, S, W, J.out, J.rows_e, J.kw, blk, l,
+        oz_slice_tile<T, MODE_CA, BF3>(X, J.g, J.exps, S, J.out, J.rows_e, J.kw, blk, l,
                                        *reinterpret_cast<SliceSmemOf<T, MODE_CA> *>(&sm));
         break;
     default:
-        oz_slice_tile<T, MODE_CB, BF3>(X, J.g, J.exps, S, W, J.out, J.rows_e, J.kw, blk, l,
+        oz_slice_tile<T, MODE_CB, BF3>(X, J.g, J.exps, S, J.out, J.rows_e, J.kw, blk, l,
                                        *reinterpret_cast<SliceSmemOf<T, MODE_CB> *>(&sm));
         break;
     }
 }
 
-__global__ void __launch_bounds__(256, 4) k_oz_pre_multi(const PreJob *__restrict__ jobs,
+__global__ void __launch_bounds__(256, 3) k_oz_pre_multi(const PreJob *__restrict__ jobs,
                                                          const int64_t *__restrict__ start, int njobs, int phase) {
     __shared__ __align__(16) PreSmem sm;
     const int64_t b = blockIdx.x;
@@ -1862,15 +1971,14 @@ __global__ void __launch_bounds__(256, 4) k_oz_pre_multi(const PreJob *__restric
             if (S == 0) return;  // the plain form will run this contraction
         }
         if (J.bf3) {
-            if (J.dtype == MGB_C32) pre_slice_typed<float2, true>(J, 3, 0, blk, l, sm);
-            else pre_slice_typed<float, true>(J, 3, 0, blk, l, sm);
+            if (J.dtype == MGB_C32) pre_slice_typed<float2, true>(J, 3, blk, l, sm);
+            else pre_slice_typed<float, true>(J, 3, blk, l, sm);
         } else {
-            const int W = oz_digit_bits(S);
             switch (J.dtype) {
-            case MGB_F64: pre_slice_typed<double, false>(J, S, W, blk, l, sm); break;
-            case MGB_C64: pre_slice_typed<double2, false>(J, S, W, blk, l, sm); break;
-            case MGB_F32: pre_slice_typed<float, false>(J, S, W, blk, l, sm); break;
-            default: pre_slice_typed<float2, false>(J, S, W, blk, l, sm); break;
+            case MGB_F64: pre_slice_typed<double, false>(J, S, blk, l, sm); break;
+            case MGB_C64: pre_slice_typed<double2, false>(J, S, blk, l, sm); break;
+            case MGB_F32: pre_slice_typed<float, false>(J, S, blk, l, sm); break;
+            default: pre_slice_typed<float2, false>(J, S, blk, l, sm); break;
             }
         }
     }
@@ -1883,9 +1991,26 @@ __global__ void k_gather_sel(const int32_t *const *__restrict__ src, int32_t *__
 }
 
 // One block per adaptive contraction (the body of k_oz_choose).
-__global__ void __launch_bounds__(1024) k_oz_choose_multi(const ChooseJob *__restrict__ jobs) {
-    const ChooseJob &c = jobs[blockIdx.x];
-    oz_choose_body(c.st, c.qa, c.qb, c.pa, c.pb, c.K, c.L, c.cand, c.tol, c.margin, c.cx);
+// The estimate's sums of every adaptive contraction of a batch: job j owns
+// blocks [start[j], start[j + 1]) (oz_est_blocks(K) per batch entry).
+__global__ void __launch_bounds__(256) k_oz_est_multi(const ChooseJob *__restrict__ jobs,
+                                                      const int64_t *__restrict__ start, int njobs) {
+    __shared__ double red[2][8];
+    const int64_t b = blockIdx.x;
+    int lo = 0, hi = njobs - 1;  // the last job whose first block is <= b
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (start[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const ChooseJob &c = jobs[lo];
+    const int64_t local = b - start[lo], nb = oz_est_blocks(c.K), l = local / nb;
+    oz_est_block(c.st, c.qa, c.qb, c.pa, c.pb, c.K, local - l * nb, l, red);
+}
+// One thread per adaptive contraction: its estimate and choice.
+__global__ void k_oz_choose_multi(const ChooseJob *__restrict__ jobs, int njobs) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < njobs) oz_choose_final(jobs[j].st, jobs[j].cand, jobs[j].tol, jobs[j].margin, jobs[j].cx);
 }
 
 struct OzBatchBuffers {
@@ -1944,7 +2069,6 @@ static void fill_prejob(PreJob &J, const ContractionPlan &p, int t, const void *
     J.rows_e = t == 0 ? p.m_e : p.n_e;
     J.kw = p.kpad / 2;
     const int64_t R = J.g.R, K = p.K, L = p.L;
-    const int KT = J.mode == MODE_REAL ? 64 : 32;
     int64_t zw = 0;
     if (exact) {
         J.zero[0] = J.exps;
@@ -1966,10 +2090,9 @@ static void fill_prejob(PreJob &J, const ContractionPlan &p, int t, const void *
         }
     }
     J.tiles[PRE_ZERO] = zw ? std::min<int64_t>((zw + 1023) / 1024, 64) : 0;
-    const int64_t tiles32 = ((R + 31) / 32) * ((K + 31) / 32) * L;
-    J.tiles[PRE_SCALE] = exact ? tiles32 : 0;
+    J.tiles[PRE_SCALE] = exact ? ((R + 31) / 32) * ((K + OZ_SCAN_KT - 1) / OZ_SCAN_KT) * L : 0;
     J.tiles[PRE_STAT] = (exact && p.adaptive) ? oz_stat_blocks(R, K) * L : 0;
-    J.tiles[PRE_SLICE] = ((R + 31) / 32) * ((K + KT - 1) / KT) * L;
+    J.tiles[PRE_SLICE] = ((R + 31) / 32) * ((K + OZ_SLICE_KT - 1) / OZ_SLICE_KT) * L;
 }
 
 int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *buf, cudaStream_t s,
@@ -2021,7 +2144,8 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
             gem[std::make_tuple(exact ? p.slices : 3, exact ? 1 : 0, cx ? 1 : 0)].push_back(job);
         }
     }
-    // ---- one staging area: [pre jobs][pre starts x 4 phases][choose jobs][per variant: jobs, starts][sel]
+    // ---- one staging area: [pre jobs][pre starts x 4 phases][choose jobs, their estimate blocks' starts]
+    //      [per item: fixed slice count, address of its slice count][per variant: jobs, starts]
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     size_t off = 0;
     const size_t o_pre = off;
@@ -2030,6 +2154,8 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
     off = al(off + PRE_PHASES * (pre.size() + 1) * sizeof(int64_t));
     const size_t o_ch = off;
     off = al(off + choose.size() * sizeof(ChooseJob));
+    const size_t o_cs = off;
+    off = al(off + (choose.size() + 1) * sizeof(int64_t));
     // per item: the address of its slice count (adaptive: the choice; else
     // the fixed count stored here)
     const size_t o_fix = off;
@@ -2055,6 +2181,10 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
         blocks[ph] = st[pre.size()];
     }
     std::memcpy(h + o_ch, choose.data(), choose.size() * sizeof(ChooseJob));
+    int64_t *cst = (int64_t *)(h + o_cs);
+    cst[0] = 0;
+    for (size_t j = 0; j < choose.size(); ++j) cst[j + 1] = cst[j] + oz_est_blocks(choose[j].K) * choose[j].L;
+    const int64_t est_blocks = cst[choose.size()];
     for (int i = 0; i < n; ++i) {
         const ContractionPlan &p = *items[i].p;
         ((int32_t *)(h + o_fix))[i] = p.form == MGB_FORM_OZAKI ? p.slices : 3;
@@ -2078,7 +2208,14 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
     const PreJob *dpre = (const PreJob *)(d + o_pre);
     for (int ph = 0; ph < PRE_PHASES; ++ph) {
         if (ph == PRE_SLICE && !choose.empty()) {
-            k_oz_choose_multi<<<(unsigned)choose.size(), 1024, 0, s>>>((const ChooseJob *)(d + o_ch));
+            if (est_blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "batch: estimate grid too large");
+            if (est_blocks > 0) {
+                k_oz_est_multi<<<(unsigned)est_blocks, 256, 0, s>>>((const ChooseJob *)(d + o_ch),
+                                                                    (const int64_t *)(d + o_cs), (int)choose.size());
+                MGB_CUDA_CHECK(cudaGetLastError());
+            }
+            const int nc = (int)choose.size();
+            k_oz_choose_multi<<<(nc + 127) / 128, 128, 0, s>>>((const ChooseJob *)(d + o_ch), nc);
             MGB_CUDA_CHECK(cudaGetLastError());
         }
         if (blocks[ph] == 0) continue;
