@@ -417,7 +417,7 @@ __device__ __forceinline__ void oz_scale_tile(const T *__restrict__ X, const OpG
     }
 }
 template <typename T>
-__global__ void __launch_bounds__(256) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps, int32_t *emax,
+__global__ void __launch_bounds__(256, 4) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps, int32_t *emax,
                                                   int2 *part) {
     __shared__ ScaleSmem sm;
     oz_scale_tile<T>(X, g, exps, emax, part, blockIdx.x, blockIdx.y, sm);
@@ -647,11 +647,12 @@ __device__ __forceinline__ float oz_digit_f(int64_t Qb) {
         return NEG ? c - m : m - c;
     }
 }
-// Two floats that bf16 holds exactly (the digits) as one packed word, `lo`
-// in the low half: one conversion instruction.
+// Two floats that bf16 holds exactly (the digits: integers of at most 8
+// significant bits) as one packed word, `lo` in the low half. Their bf16
+// bits are the upper halves of their float bits, so one byte permute on the
+// integer pipe packs them (no conversion instruction).
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<uint32_t *>(&v);
+    return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
 }
 // f(integral_constant<int, s>) for s = 0 .. N-1, unrolled at compile time.
 template <int N, int s = 0, typename F>
@@ -739,10 +740,11 @@ __device__ __forceinline__ void oz_write_pieces(const SliceSmemOf<T, MODE> &sm, 
                 if (word >= kw) continue;
                 // MODE_CA: row r; MODE_CB: rows 2r (re, -im) and 2r + 1 (im, re)
                 uint32_t *o = outl + (MODE == MODE_CB ? 2 * row : row) * kw + word;
+                const T v = sm.tile[r][kk];
                 uint32_t pr[8], pi[8], pn[8];
-                bf3_pieces((float)OzIn<T>::re(sm.tile[r][kk]), pr);
-                bf3_pieces((float)OzIn<T>::im(sm.tile[r][kk]), pi);
-                bf3_pieces(-(float)OzIn<T>::im(sm.tile[r][kk]), pn);
+                bf3_pieces((float)OzIn<T>::re(v), pr);
+                bf3_pieces((float)OzIn<T>::im(v), pi);
+                bf3_pieces(-(float)OzIn<T>::im(v), pn);
 #pragma unroll
                 for (int s = 0; s < 3; ++s) {
                     if (MODE == MODE_CA) {
@@ -790,8 +792,9 @@ __device__ __forceinline__ void oz_write_digits(const SliceSmemOf<T, MODE> &sm, 
                 const int64_t word = k0 + kk;
                 if (word >= kw) continue;
                 uint32_t *o = outl + (MODE == MODE_CB ? 2 * row : row) * kw + word;
-                const int64_t qr = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(sm.tile[r][kk]), e) + bias;
-                const int64_t qi = oz_fixed(bad ? 0.0 : (double)OzIn<T>::im(sm.tile[r][kk]), e) + bias;
+                const T v = sm.tile[r][kk];  // one shared-memory read of the whole element
+                const int64_t qr = oz_fixed(bad ? 0.0 : (double)OzIn<T>::re(v), e) + bias;
+                const int64_t qi = oz_fixed(bad ? 0.0 : (double)OzIn<T>::im(v), e) + bias;
                 oz_static_for<S>([&](auto sc) {
                     constexpr int s = decltype(sc)::value;
                     const float dr = oz_digit_f<W, s>(qr), di = oz_digit_f<W, s>(qi);
