@@ -67,6 +67,7 @@
 #include <vector>
 
 #include "mgb_internal.h"
+#include "mgb_ptx.h"
 #include "mgb_x96.h"
 
 namespace mgb {
@@ -93,7 +94,6 @@ constexpr int OZ_ISSUER2_WARP = 2 + OZ_EPI_WARPS;
 constexpr int OZ_A_TILE = OZ_BM * OZ_BK * 2;  // 8192 bytes per slice
 constexpr int OZ_SMEM_BUDGET = 220 * 1024;
 constexpr int OZ_MAX_STAGES = 6;
-constexpr long long OZ_TIMEOUT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 // Columns per digit group (= embedded rows of B per CTA): two banks of S
 // groups must fit the 512 TMEM columns, and one MMA covers at most 256.
@@ -127,54 +127,6 @@ static_assert(2 * oz_smem_bytes(3, true) > 228 * 1024 && 2 * oz_smem_bytes(8, tr
 // =============================================================================
 // PTX wrappers
 // =============================================================================
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: false when the CTA aborted or this wait timed out (about a
-// second of clock64 cycles, checked every 256 tries).
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag,
-                                          int32_t *status) {
-    if (mbar_try(bar, parity)) return true;
-    long long t0 = clock64();
-    for (uint32_t n = 1;; ++n) {
-        if (mbar_try(bar, parity)) return true;
-        if ((n & 255) == 0) {
-            if (*abort_flag) return false;
-            if (clock64() - t0 > OZ_TIMEOUT_CYCLES) {
-                *abort_flag = 1;
-                atomicCAS(status, 0, (int32_t)MGB_ERR_DEVICE_TIMEOUT);
-                return false;
-            }
-        }
-    }
-}
-// Drain wait used after an abort: bounded, never raises the abort flag.
-__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
-    long long t0 = clock64();
-    while (!mbar_try(bar, parity))
-        if (clock64() - t0 > OZ_TIMEOUT_CYCLES) return;
-}
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *tm, int c0, int c1,
                                             int c2, uint32_t bar) {
     asm volatile(
@@ -1464,12 +1416,7 @@ static uint64_t stat_bytes(const ContractionPlan &p) {
     return align256(align256(sizeof(OzStats) + 2 * (uint64_t)p.L * 4) + 2 * (uint64_t)p.L * p.K * 4);
 }
 
-typedef CUresult (*PFN_encodeTiled_t)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                      const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                      const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                      CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static PFN_encodeTiled_t encode_fn() {
+PFN_encodeTiled_t tensor_map_encoder() {
     static PFN_encodeTiled_t fn = nullptr;
     static std::once_flag once;
     std::call_once(once, [] {
@@ -1485,7 +1432,7 @@ static PFN_encodeTiled_t encode_fn() {
 
 static int make_map(CUtensorMap *tm, void *base, int64_t k_e, int64_t rows, int64_t planes,
                     int64_t kpad, int box_rows, int S) {
-    PFN_encodeTiled_t enc = encode_fn();
+    PFN_encodeTiled_t enc = tensor_map_encoder();
     if (!enc) return fail(MGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[3] = {(cuuint64_t)k_e, (cuuint64_t)rows, (cuuint64_t)planes};
     cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)(kpad * 2 * rows)};

@@ -15,6 +15,7 @@
 #include <type_traits>
 
 #include "mgb_internal.h"
+#include "mgb_ptx.h"
 
 namespace mgb {
 
@@ -169,6 +170,237 @@ __global__ void __launch_bounds__(256) k_transpose_v2(const T *__restrict__ x, T
     }
 }
 
+// ---- TMA-staged transpose (same-type 8- and 16-byte elements) -----------------
+// A tile is 32 R rows of a (Y's unit-stride mode; R = 1..4, whichever pads
+// a's extent least) by 128 bytes of b (X's unit-stride mode: 16 Float64 /
+// ComplexF32 or 8 ComplexF64 elements). One 5-D TMA box per tile (b, a and
+// up to three outer modes, X's own strides) lands in a ring of stages with
+// the 128-byte swizzle: 16-byte chunk j of tile row r sits at
+// r * 128 + ((j ^ (r % 8)) * 16), so the 8 lanes of a quarter warp, reading
+// one chunk of 8 consecutive rows, hit 8 different bank groups.
+// A persistent grid walks the tiles t = b, b + grid, ...; the producer
+// thread steps the tile coordinates by the grid size in mixed radix (one
+// add and compare per digit, no division), issues the load and publishes
+// the tile's Y offset beside the stage. Four warps read each tile
+// column-wise:
+//  * 16-byte elements: lane l reads row l of a chunk (one element) and the
+//    warp stores 32 consecutive elements of a Y column, 512 bytes;
+//  * 8-byte elements: lane l reads row l of a chunk (elements b, b + 1);
+//    lanes l and l ^ 1 swap one element by a shuffle, so that the even lane
+//    holds column b and the odd lane column b + 1 for rows (l & ~1, l | 1),
+//    and every lane stores one 16-byte pair of a Y column.
+// Loads never wait for stores, so each SM keeps several tiles of reads in
+// flight while it writes the previous ones. Rows past a's extent arrive
+// zero-filled from the TMA box and are not stored.
+static ModeGroup drop_mode(const ModeGroup &g, int a, int b);
+
+constexpr int kTmaConsumers = 4;  // warps
+constexpr int kTmaThreads = 32 * (kTmaConsumers + 1);
+
+struct TmaPermArgs {
+    int64_t ext[5];   // tiles along b, tiles along a, outer extents (1 past n)
+    int64_t ystr[3];  // Y strides of the outer modes
+    int64_t ea, eb, syb;
+    int64_t tiles;
+};
+struct TmaTileInfo {
+    int64_t yoff;  // Y offset (elements) of the tile's first row and column
+    int32_t rows, cols;  // rows of a and columns of b inside the tensor
+};
+
+__host__ __device__ constexpr int tma_stages(int R) { return R == 1 ? 8 : R == 2 ? 4 : R == 3 ? 3 : 2; }
+__host__ __device__ constexpr int tma_tile_bytes(int R) { return 32 * R * 128; }
+__host__ __device__ constexpr int tma_smem_bytes(int R) {
+    return tma_stages(R) * (tma_tile_bytes(R) + (int)sizeof(TmaTileInfo) + 16) + 1024 /*align*/ + 16;
+}
+
+template <int ES, int R>
+__global__ void __launch_bounds__(kTmaThreads) k_transpose_tma(const __grid_constant__ CUtensorMap tm,
+                                                               unsigned char *__restrict__ y, const TmaPermArgs p,
+                                                               int32_t *status) {
+    static_assert(ES == 8 || ES == 16, "8- or 16-byte elements");
+    constexpr int NST = tma_stages(R);
+    constexpr int TB = tma_tile_bytes(R);
+    constexpr int BI = 128 / ES;  // elements of b per tile
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *ring = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    TmaTileInfo *info = (TmaTileInfo *)(ring + NST * TB);
+    uint64_t *full = (uint64_t *)(info + NST);
+    uint64_t *empty = full + NST;
+    volatile int *abort_flag = (volatile int *)(empty + NST);
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(smem_u32(full + s), 1);
+            mbar_init(smem_u32(empty + s), kTmaConsumers);
+        }
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == kTmaConsumers) {
+        // ---------------- TMA producer ----------------
+        if (lane != 0) return;
+        // coordinates of tile blockIdx.x and of the step gridDim.x, mixed radix
+        int64_t c[5], st[5];
+        int64_t u = blockIdx.x, v = gridDim.x;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            const int64_t qu = u / p.ext[i], qv = v / p.ext[i];
+            c[i] = u - qu * p.ext[i];
+            st[i] = v - qv * p.ext[i];
+            u = qu;
+            v = qv;
+        }
+        uint32_t g = 0;  // tiles issued by this CTA
+        for (int64_t t = blockIdx.x; t < p.tiles; t += gridDim.x, ++g) {
+            const int s = (int)(g % NST);
+            const uint32_t round = g / NST;
+            if (!mbar_wait(smem_u32(empty + s), (round & 1) ^ 1, abort_flag, status)) break;
+            const int64_t a0 = c[1] * 32 * R, b0 = c[0] * BI;
+            TmaTileInfo ti;
+            ti.yoff = c[2] * p.ystr[0] + c[3] * p.ystr[1] + c[4] * p.ystr[2] + a0 + b0 * p.syb;
+            ti.rows = (int32_t)min(p.ea - a0, (int64_t)(32 * R));
+            ti.cols = (int32_t)min(p.eb - b0, (int64_t)BI);
+            info[s] = ti;
+            const uint32_t fb = smem_u32(full + s);
+            mbar_expect_tx(fb, TB);  // release: the consumers see info[s] after their wait
+            // x coordinate in 8-byte units: c[0] * 16, a multiple of 16 bytes
+            tma_load_5d(smem_u32(ring + s * TB), &tm, (int)(c[0] * 16), (int)a0, (int)c[2], (int)c[3], (int)c[4],
+                        fb);
+            // next tile: add the step digit by digit with carries
+            int64_t carry = 0;
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {
+                c[i] += st[i] + carry;
+                carry = c[i] >= p.ext[i];
+                if (carry) c[i] -= p.ext[i];
+            }
+        }
+        // no bulk copy may still be writing into shared memory at exit
+        for (uint32_t gg = g > (uint32_t)NST ? g - NST : 0u; gg < g; ++gg)
+            mbar_drain(smem_u32(full + gg % NST), (gg / NST) & 1);
+        return;
+    }
+
+    // ---------------- consumers ----------------
+    // Warp w reads the (row block, chunk) pairs q = w + 4 i, i < 2 R:
+    // row block q % R, 16-byte chunk q / R.
+    uint32_t g = 0;
+    for (int64_t t = blockIdx.x; t < p.tiles; t += gridDim.x, ++g) {
+        const int s = (int)(g % NST);
+        const uint32_t round = g / NST;
+        if (!__all_sync(0xffffffffu, mbar_wait(smem_u32(full + s), round & 1, abort_flag, status))) break;
+        const TmaTileInfo ti = info[s];
+        const unsigned char *tile = ring + s * TB;
+#pragma unroll
+        for (int i = 0; i < 2 * R; ++i) {
+            const int q = warp + 4 * i;
+            const int row = (q % R) * 32 + lane;
+            const int j = q / R;
+            const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(tile + row * 128 + ((j ^ (row & 7)) << 4));
+            if constexpr (ES == 16) {
+                if (row < ti.rows && j < ti.cols)
+                    *reinterpret_cast<ulonglong2 *>(y + (ti.yoff + row + j * p.syb) * ES) = v;
+            } else {
+                const bool odd = lane & 1;
+                const unsigned long long got = __shfl_xor_sync(0xffffffffu, odd ? v.x : v.y, 1);
+                const int r0 = row & ~1, col = 2 * j + (odd ? 1 : 0);
+                if (r0 < ti.rows && col < ti.cols) {
+                    unsigned char *dst = y + (ti.yoff + r0 + col * p.syb) * ES;
+                    if (r0 + 1 < ti.rows)
+                        *reinterpret_cast<ulonglong2 *>(dst) = odd ? make_ulonglong2(got, v.y)
+                                                                   : make_ulonglong2(v.x, got);
+                    else
+                        *reinterpret_cast<unsigned long long *>(dst) = odd ? got : v.x;
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(empty + s));
+    }
+}
+
+// Tries the TMA-staged transpose; returns 1 when it does not apply (the
+// caller then uses the register-tiled kernels), else an mgb_status.
+template <int ES>
+static int try_transpose_tma(const ModeGroup &g, int bmode, const void *x, void *y, cudaStream_t s) {
+    const int64_t ea = g.ext[0], eb = g.ext[bmode];
+    const int64_t sxa = g.str[0][0], syb = g.str[1][bmode];
+    ModeGroup outer = drop_mode(g, 0, bmode);
+    if (outer.n > 3) return 1;
+    if ((uintptr_t)x % 16 || (uintptr_t)y % 16) return 1;
+    if (ea >= INT32_MAX || eb * (ES / 8) >= INT32_MAX) return 1;
+    // box strides: positive multiples of 16 bytes below 2^40; Y pairs 16-byte aligned
+    auto ok_x = [](int64_t st) { return st > 0 && (st * ES) % 16 == 0 && st * ES < (1ll << 40); };
+    auto ok_y = [](int64_t st) { return st > 0 && (st * ES) % 16 == 0; };
+    if (!ok_x(sxa) || !ok_y(syb)) return 1;
+    for (int i = 0; i < outer.n; ++i)
+        if (!ok_x(outer.str[0][i]) || !ok_y(outer.str[1][i]) || outer.ext[i] >= INT32_MAX) return 1;
+    // outer modes by increasing X stride
+    std::vector<int> ord(outer.n);
+    for (int i = 0; i < outer.n; ++i) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](int u, int v) { return outer.str[0][u] < outer.str[0][v]; });
+    // 32 R rows per tile, R = 1..4: the least padding of a's extent, the
+    // larger tile on ties
+    int R = 4;
+    for (int r = 3; r >= 1; --r)
+        if ((ea + 32 * r - 1) / (32 * r) * (32 * r) < (ea + 32 * R - 1) / (32 * R) * (32 * R)) R = r;
+    TmaPermArgs a;
+    a.ext[0] = (eb + 128 / ES - 1) / (128 / ES);
+    a.ext[1] = (ea + 32 * R - 1) / (32 * R);
+    for (int i = 0; i < 3; ++i) {
+        a.ext[2 + i] = i < outer.n ? outer.ext[ord[i]] : 1;
+        a.ystr[i] = i < outer.n ? outer.str[1][ord[i]] : 0;
+    }
+    a.ea = ea;
+    a.eb = eb;
+    a.syb = syb;
+    a.tiles = a.ext[0] * a.ext[1] * a.ext[2] * a.ext[3] * a.ext[4];
+
+    PFN_encodeTiled_t enc = tensor_map_encoder();
+    if (!enc) return 1;
+    cuuint64_t dims[5], strides[4];
+    dims[0] = (cuuint64_t)(eb * (ES / 8));  // 8-byte units
+    dims[1] = (cuuint64_t)ea;
+    strides[0] = (cuuint64_t)(sxa * ES);
+    for (int i = 0; i < 3; ++i) {
+        dims[2 + i] = (cuuint64_t)a.ext[2 + i];
+        strides[1 + i] = i < outer.n ? (cuuint64_t)(outer.str[0][ord[i]] * ES) : strides[i];
+    }
+    cuuint32_t box[5] = {16, (cuuint32_t)(32 * R), 1, 1, 1};
+    cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    CUtensorMap tm;
+    if (enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, const_cast<void *>(x), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return 1;
+    int32_t *status = device_status_ptr();
+    if (!status) return fail(MGB_ERR_CUDA, "device status word unavailable");
+
+    auto launch = [&](auto kern, int smem) -> int {
+        int dev = 0, sms = 0, per_sm = 0;
+        MGB_CUDA_CHECK(cudaGetDevice(&dev));
+        MGB_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        MGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTmaThreads, smem));
+        const int64_t grid = std::min<int64_t>(a.tiles, (int64_t)sms * std::max(per_sm, 1));
+        kern<<<(unsigned)grid, kTmaThreads, smem, s>>>(tm, (unsigned char *)y, a, status);
+        MGB_CUDA_CHECK(cudaGetLastError());
+        return MGB_OK;
+    };
+    static_assert(tma_smem_bytes(1) <= 48 * 1024 && tma_smem_bytes(2) <= 48 * 1024 &&
+                      tma_smem_bytes(3) <= 48 * 1024 && tma_smem_bytes(4) <= 48 * 1024,
+                  "default dynamic shared memory limit");
+    switch (R) {
+    case 1: return launch(k_transpose_tma<ES, 1>, tma_smem_bytes(1));
+    case 2: return launch(k_transpose_tma<ES, 2>, tma_smem_bytes(2));
+    case 3: return launch(k_transpose_tma<ES, 3>, tma_smem_bytes(3));
+    default: return launch(k_transpose_tma<ES, 4>, tma_smem_bytes(4));
+    }
+}
+
 // ---- gather (no unit-stride mode) ---------------------------------------------
 template <typename TS, typename TD>
 __global__ void k_gather(const TS *__restrict__ x, TD *__restrict__ y, ModeGroup g, int64_t total) {
@@ -229,6 +461,10 @@ static int run_permute(const PermGeom &pg, const TS *x, TD *y, cudaStream_t s) {
         // least (a 96-wide panel is three 32-row tiles, not one and a half
         // 64-row ones whose second half idles), larger on ties; 16-byte
         // types stay at 32 x 32 (16 KB of shared memory).
+        if constexpr (std::is_same<TS, TD>::value && (sizeof(TD) == 8 || sizeof(TD) == 16)) {
+            const int rc = try_transpose_tma<(int)sizeof(TD)>(g, pg.b, x, y, s);
+            if (rc != 1) return rc;
+        }
         if constexpr (std::is_same<TS, TD>::value && sizeof(TD) == 8) {
             // 16-byte vectors: every tile row starts on a 16-byte boundary in
             // X (row stride sxa, tile columns from an even b) and in Y
