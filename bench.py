@@ -100,6 +100,11 @@ class Clocks:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once sampling runs (nvidia-smi takes a
+            # moment to start), so that its samples cover all of it
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -996,6 +1001,60 @@ def main():
     value = flops * ws * args.steps / (ms / 1e3) / 1e12
     launches_per_step = 5  # 2 exponent scans, 2 slicers, 1 tcgen05 GEMM (plus 2 memsets)
 
+    # End to end through the public API with host buffers: every step copies
+    # its inputs from pinned host memory, contracts, and copies the result back.
+    # Steps are pipelined over two device buffer sets: the host->device copy of
+    # step i + 1 and the device->host copy of step i - 1 run on their own
+    # streams while step i computes (byte-for-byte copies of the column-major
+    # arrays as flat buffers).
+    cset = []
+    for _ in range(2):
+        af = torch.empty(a_f.numel(), dtype=torch.complex128, device=dev)
+        bf = torch.empty(b_f.numel(), dtype=torch.complex128, device=dev)
+        cf = torch.empty(n * n, dtype=torch.complex128, device=dev)
+        ch = torch.empty(n * n, dtype=torch.complex128).pin_memory()
+        cset.append((af, bf, cf, ch))
+    h2d, d2h = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    ev = {k: [torch.cuda.Event(), torch.cuda.Event()] for k in ("in", "out", "comp")}
+
+    def e2e_run(nsteps):
+        h2d.wait_stream(stream)  # no copy starts before the timer
+        for i in range(nsteps):
+            bset = i % 2
+            af, bf, cf, ch = cset[bset]
+            h2d.wait_event(ev["comp"][bset])  # step i - 2 has finished reading this set
+            with torch.cuda.stream(h2d):
+                af.copy_(a_f, non_blocking=True)
+                bf.copy_(b_f, non_blocking=True)
+                ev["in"][bset].record(h2d)
+            stream.wait_event(ev["in"][bset])
+            stream.wait_event(ev["out"][bset])  # step i - 2's result has left this set
+            _lib.check(lib.mgb_contract(plan.handle, af.data_ptr(), bf.data_ptr(), cf.data_ptr(), ws_t.data_ptr(),
+                                        ws_t.numel(), stream.cuda_stream), lib)
+            ev["comp"][bset].record(stream)
+            d2h.wait_event(ev["comp"][bset])
+            with torch.cuda.stream(d2h):
+                ch.copy_(cf, non_blocking=True)
+                ev["out"][bset].record(d2h)
+        for bset in range(2):
+            stream.wait_event(ev["out"][bset])
+
+    e2e_run(2)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk_e2e:
+        ee0.record(stream)
+        e2e_run(args.steps)
+        ee1.record(stream)
+        torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(ee0.elapsed_time(ee1), ws)
+    e2e = flops * ws * args.steps / (e2e_ms / 1e3) / 1e12
+    # the last step's host copy (what the caller receives) against the device-timed result
+    e2e_ok = bool(torch.equal(cset[(args.steps - 1) % 2][3].view(n, n), C.t().cpu()))
+    del cset
+    torch.cuda.empty_cache()
+
     # kernel timing for the roofline: phase events around the GEMM launch
     lib.mgb_plan_set_timing(plan.handle, 1)
     pre, mainv = [], []
@@ -1057,58 +1116,6 @@ def main():
            "rel_err_reference": "plain FP64 DMMA on the ComplexF32 inputs widened"}
     del A32, B32, C32, ws32
 
-    # End to end through the public API with host buffers: every step copies
-    # its inputs from pinned host memory, contracts, and copies the result back.
-    # Steps are pipelined over two device buffer sets: the host->device copy of
-    # step i + 1 and the device->host copy of step i - 1 run on their own
-    # streams while step i computes (byte-for-byte copies of the column-major
-    # arrays as flat buffers).
-    cset = []
-    for _ in range(2):
-        af = torch.empty(a_f.numel(), dtype=torch.complex128, device=dev)
-        bf = torch.empty(b_f.numel(), dtype=torch.complex128, device=dev)
-        cf = torch.empty(n * n, dtype=torch.complex128, device=dev)
-        ch = torch.empty(n * n, dtype=torch.complex128).pin_memory()
-        cset.append((af, bf, cf, ch))
-    h2d, d2h = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    ev = {k: [torch.cuda.Event(), torch.cuda.Event()] for k in ("in", "out", "comp")}
-
-    def e2e_run(nsteps):
-        h2d.wait_stream(stream)  # no copy starts before the timer
-        for i in range(nsteps):
-            bset = i % 2
-            af, bf, cf, ch = cset[bset]
-            h2d.wait_event(ev["comp"][bset])  # step i - 2 has finished reading this set
-            with torch.cuda.stream(h2d):
-                af.copy_(a_f, non_blocking=True)
-                bf.copy_(b_f, non_blocking=True)
-                ev["in"][bset].record(h2d)
-            stream.wait_event(ev["in"][bset])
-            stream.wait_event(ev["out"][bset])  # step i - 2's result has left this set
-            _lib.check(lib.mgb_contract(plan.handle, af.data_ptr(), bf.data_ptr(), cf.data_ptr(), ws_t.data_ptr(),
-                                        ws_t.numel(), stream.cuda_stream), lib)
-            ev["comp"][bset].record(stream)
-            d2h.wait_event(ev["comp"][bset])
-            with torch.cuda.stream(d2h):
-                ch.copy_(cf, non_blocking=True)
-                ev["out"][bset].record(d2h)
-        for bset in range(2):
-            stream.wait_event(ev["out"][bset])
-
-    e2e_run(2)
-    torch.cuda.synchronize()
-    barrier(ws)
-    ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ee0.record(stream)
-    e2e_run(args.steps)
-    ee1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(ee0.elapsed_time(ee1), ws)
-    e2e = flops * ws * args.steps / (e2e_ms / 1e3) / 1e12
-    # the last step's host copy (what the caller receives) against the device-timed result
-    e2e_ok = bool(torch.equal(cset[(args.steps - 1) % 2][3].view(n, n), C.t().cpu()))
-    status = m.device_status(dev)
-
     # batching form: a PEPS group of 1024 instances (the full one is --workload peps)
     peps = peps_bench(dev, 1024, quick=True, check=8)
     torch.cuda.empty_cache()
@@ -1117,10 +1124,11 @@ def main():
     torch.cuda.empty_cache()
 
     # served mixed-size stream (short sweep; the full one is --workload serve)
-    del cset, a_f, b_f
+    del a_f, b_f
     torch.cuda.empty_cache()
     serving = serve_bench(dev, [1000, 3000, 10000, 30000, 100000], 1.0, n_requests=2048, quick=True)
 
+    status = m.device_status(dev)
     cpu = None
     if rank == 0 and ws == 1:
         cpu = cpu_sample(n, args.cpu_seconds)
@@ -1142,7 +1150,7 @@ def main():
             "e2e": {"value": e2e, "unit": "TFLOP/s", "ms_per_step": e2e_ms / args.steps,
                     "h2d_bytes_per_step": A.numel() * 16 + B.numel() * 16, "d2h_bytes_per_step": C.numel() * 16,
                     "pipelined": "copies of step i+1 / i-1 overlap step i (two buffer sets, copy streams)",
-                    "result_matches_device_run": e2e_ok},
+                    "result_matches_device_run": e2e_ok, "clocks": clk_e2e.summary()},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": achieved / bf16_peak, "traffic": traffic, "peak_kind": f"bf16 dense burst ({peak_kind})",
                          "kernel": "k_oz_gemm", "kernel_ms": gemm_ms, "prepass_ms": statistics.mean(pre),

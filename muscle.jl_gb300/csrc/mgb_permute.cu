@@ -4,10 +4,13 @@
 // After folding, the copy is one of:
 //  * row copy   — the fastest mode of Y is also unit-stride in X: contiguous
 //                 rows, copied with 128-bit vectors when aligned;
-//  * transpose  — X and Y have different unit-stride modes: shared-memory
-//                 tiles with edges of 32 or 64 elements (32 x 32 for 16-byte
-//                 types), coalesced on both sides, other modes enumerated by
-//                 the grid;
+//  * transpose  — X and Y have different unit-stride modes. Same-type 8- and
+//                 16-byte elements whose strides TMA can address (at most
+//                 three other modes, strides in multiples of 16 bytes) go
+//                 through TMA-staged tiles (k_transpose_tma); the rest use
+//                 register-staged shared-memory tiles with edges of 32 or 64
+//                 elements (32 x 32 for 16-byte types), coalesced on both
+//                 sides, other modes enumerated by the grid;
 //  * gather     — strided views without a unit-stride mode: element-wise.
 // HBM-bound: algorithmic bytes = numel * (sizeof(src) + sizeof(dst)).
 #include <algorithm>
