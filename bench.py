@@ -984,6 +984,90 @@ def main():
     def step(p=plan, out=C):
         launch(p, out)
 
+    # End to end through the public API with host buffers: every step copies
+    # its inputs from pinned host memory, contracts, and copies the result back
+    # (byte-for-byte copies of the column-major arrays as flat buffers).
+    # Steps alternate between two device buffer sets. One copy stream carries
+    # both directions in order: once step i has computed, its result goes back
+    # and then step i + 2's inputs come in, while step i + 1 computes (about
+    # 15 ms of copies at ~200 GB/s against about 78 ms of compute). This runs
+    # before the device-timed loop and its clock sampler: on GB300, host copies
+    # in the first few hundred milliseconds after nvidia-smi started ran at a
+    # tenth of their usual rate.
+    cset = []
+    for _ in range(2):
+        af = torch.empty(a_f.numel(), dtype=torch.complex128, device=dev)
+        bf = torch.empty(b_f.numel(), dtype=torch.complex128, device=dev)
+        cf = torch.empty(n * n, dtype=torch.complex128, device=dev)
+        ch = torch.empty(n * n, dtype=torch.complex128).pin_memory()
+        cset.append((af, bf, cf, ch))
+    cps = torch.cuda.Stream(dev)
+
+    def tev():
+        return torch.cuda.Event(enable_timing=True)
+
+    def e2e_run(nsteps, log=None):
+        marks = [[tev() for _ in range(6)] for _ in range(nsteps)] if log is not None else None
+        ev_in = [torch.cuda.Event() for _ in range(nsteps)]
+        ev_comp = [torch.cuda.Event() for _ in range(nsteps)]
+
+        def h2d(i):  # on the copy stream
+            af, bf, _, _ = cset[i % 2]
+            if marks:
+                marks[i][0].record(cps)
+            af.copy_(a_f, non_blocking=True)
+            bf.copy_(b_f, non_blocking=True)
+            if marks:
+                marks[i][1].record(cps)
+            ev_in[i].record(cps)
+
+        cps.wait_stream(stream)  # no copy starts before the timer
+        with torch.cuda.stream(cps):
+            for i in range(min(2, nsteps)):
+                h2d(i)
+        for i in range(nsteps):
+            af, bf, cf, ch = cset[i % 2]
+            stream.wait_event(ev_in[i])
+            if marks:
+                marks[i][2].record(stream)
+            _lib.check(lib.mgb_contract(plan.handle, af.data_ptr(), bf.data_ptr(), cf.data_ptr(), ws_t.data_ptr(),
+                                        ws_t.numel(), stream.cuda_stream), lib)
+            if marks:
+                marks[i][3].record(stream)
+            ev_comp[i].record(stream)
+            cps.wait_event(ev_comp[i])
+            with torch.cuda.stream(cps):
+                if marks:
+                    marks[i][4].record(cps)
+                ch.copy_(cf, non_blocking=True)
+                if marks:
+                    marks[i][5].record(cps)
+                if i + 2 < nsteps:
+                    h2d(i + 2)  # into the set step i has finished with
+        stream.wait_stream(cps)
+        if log is not None:
+            log.extend(marks)
+
+    e2e_run(3)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_log = []
+    ee0.record(stream)
+    e2e_run(args.steps, e2e_log)
+    ee1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(ee0.elapsed_time(ee1), ws)
+    # per step: the host->device copies, the contraction and the device->host
+    # copy, each timed on its own stream
+    e2e_phases = {name: [round(mk[2 * j].elapsed_time(mk[2 * j + 1]), 3) for mk in e2e_log]
+                  for j, name in enumerate(("h2d_ms", "contract_ms", "d2h_ms"))}
+    e2e = plan.flops * ws * args.steps / (e2e_ms / 1e3) / 1e12
+    # the last step's host copy (what the caller receives) against the device-timed result
+    e2e_ok = bool(torch.equal(cset[(args.steps - 1) % 2][3].view(n, n), C.t().cpu()))
+    del cset
+    torch.cuda.empty_cache()
+
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -1000,60 +1084,6 @@ def main():
     flops = plan.flops
     value = flops * ws * args.steps / (ms / 1e3) / 1e12
     launches_per_step = 5  # 2 exponent scans, 2 slicers, 1 tcgen05 GEMM (plus 2 memsets)
-
-    # End to end through the public API with host buffers: every step copies
-    # its inputs from pinned host memory, contracts, and copies the result back.
-    # Steps are pipelined over two device buffer sets: the host->device copy of
-    # step i + 1 and the device->host copy of step i - 1 run on their own
-    # streams while step i computes (byte-for-byte copies of the column-major
-    # arrays as flat buffers).
-    cset = []
-    for _ in range(2):
-        af = torch.empty(a_f.numel(), dtype=torch.complex128, device=dev)
-        bf = torch.empty(b_f.numel(), dtype=torch.complex128, device=dev)
-        cf = torch.empty(n * n, dtype=torch.complex128, device=dev)
-        ch = torch.empty(n * n, dtype=torch.complex128).pin_memory()
-        cset.append((af, bf, cf, ch))
-    h2d, d2h = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    ev = {k: [torch.cuda.Event(), torch.cuda.Event()] for k in ("in", "out", "comp")}
-
-    def e2e_run(nsteps):
-        h2d.wait_stream(stream)  # no copy starts before the timer
-        for i in range(nsteps):
-            bset = i % 2
-            af, bf, cf, ch = cset[bset]
-            h2d.wait_event(ev["comp"][bset])  # step i - 2 has finished reading this set
-            with torch.cuda.stream(h2d):
-                af.copy_(a_f, non_blocking=True)
-                bf.copy_(b_f, non_blocking=True)
-                ev["in"][bset].record(h2d)
-            stream.wait_event(ev["in"][bset])
-            stream.wait_event(ev["out"][bset])  # step i - 2's result has left this set
-            _lib.check(lib.mgb_contract(plan.handle, af.data_ptr(), bf.data_ptr(), cf.data_ptr(), ws_t.data_ptr(),
-                                        ws_t.numel(), stream.cuda_stream), lib)
-            ev["comp"][bset].record(stream)
-            d2h.wait_event(ev["comp"][bset])
-            with torch.cuda.stream(d2h):
-                ch.copy_(cf, non_blocking=True)
-                ev["out"][bset].record(d2h)
-        for bset in range(2):
-            stream.wait_event(ev["out"][bset])
-
-    e2e_run(2)
-    torch.cuda.synchronize()
-    barrier(ws)
-    ee0, ee1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with Clocks(local) as clk_e2e:
-        ee0.record(stream)
-        e2e_run(args.steps)
-        ee1.record(stream)
-        torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(ee0.elapsed_time(ee1), ws)
-    e2e = flops * ws * args.steps / (e2e_ms / 1e3) / 1e12
-    # the last step's host copy (what the caller receives) against the device-timed result
-    e2e_ok = bool(torch.equal(cset[(args.steps - 1) % 2][3].view(n, n), C.t().cpu()))
-    del cset
-    torch.cuda.empty_cache()
 
     # kernel timing for the roofline: phase events around the GEMM launch
     lib.mgb_plan_set_timing(plan.handle, 1)
@@ -1149,8 +1179,9 @@ def main():
             "speedup_vs_native": value / native,
             "e2e": {"value": e2e, "unit": "TFLOP/s", "ms_per_step": e2e_ms / args.steps,
                     "h2d_bytes_per_step": A.numel() * 16 + B.numel() * 16, "d2h_bytes_per_step": C.numel() * 16,
-                    "pipelined": "copies of step i+1 / i-1 overlap step i (two buffer sets, copy streams)",
-                    "result_matches_device_run": e2e_ok, "clocks": clk_e2e.summary()},
+                    "pipelined": "result of step i, then inputs of step i + 2, on one copy stream while step i + 1 "
+                                 "computes (two buffer sets)",
+                    "result_matches_device_run": e2e_ok, "phases": e2e_phases},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": achieved / bf16_peak, "traffic": traffic, "peak_kind": f"bf16 dense burst ({peak_kind})",
                          "kernel": "k_oz_gemm", "kernel_ms": gemm_ms, "prepass_ms": statistics.mean(pre),

@@ -1252,25 +1252,65 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
                 }
             }
             if (!ok) break;
+            if constexpr (EXACT) {
+                // Four conversions at a time through the straight-line routine,
+                // so that their integer sequences interleave (one conversion
+                // alone is a chain of dependent instructions); a group with a
+                // subnormal result (rare) goes through the general routine;
+                // then the group's stores.
+                constexpr int GQ = CX ? 2 : 4;  // output columns per group
+                constexpr int NP = CX ? 2 : 1;  // parts per output column
+                const uint64_t nanb = 0x7FF8000000000000ull;
 #pragma unroll
-            for (int jj = 0; jj < NCOL; ++jj) {
-                const int64_t coff = __shfl_sync(0xffffffffu, lcoff, jj);
-                const int bc = __shfl_sync(0xffffffffu, lexp, jj);
-                if (!row_ok || bc < 0) continue;
-                const int j = CX ? 2 * jj : jj;
-                const int64_t off = rowoff + coff;
-                if (EXACT) {
-                    const bool bad = badrow || bc == 0x7FF;
-                    const int E = erow + (bc == 0 ? -1022 : bc - 1022) - W * (S + 1);
-                    const double nan = __longlong_as_double(0x7FF8000000000000LL);
-                    const double v0 = bad ? nan : x96_ldexp_rn(w0[j], w1[j], w2[j], E);
-                    if (CX) {
-                        const double v1 = bad ? nan : x96_ldexp_rn(w0[j + 1], w1[j + 1], w2[j + 1], E);
-                        ((double2 *)Cl)[off] = make_double2(v0, v1);
-                    } else {
-                        ((double *)Cl)[off] = v0;
+                for (int j0 = 0; j0 < NCOL; j0 += GQ) {
+                    uint64_t bits[GQ][NP];
+                    int Eq[GQ];
+                    bool slow = false;
+#pragma unroll
+                    for (int q2 = 0; q2 < GQ; ++q2) {
+                        const int bc = __shfl_sync(0xffffffffu, lexp, j0 + q2);
+                        Eq[q2] = erow + (bc == 0 ? -1022 : bc - 1022) - W * (S + 1);
+#pragma unroll
+                        for (int pp = 0; pp < NP; ++pp) {
+                            const int j = NP * (j0 + q2) + pp;
+                            bits[q2][pp] = x96_ldexp_bits_fast(w0[j], w1[j], w2[j], Eq[q2], slow);
+                        }
                     }
-                } else {
+                    if (slow) {
+#pragma unroll
+                        for (int q2 = 0; q2 < GQ; ++q2)
+#pragma unroll
+                            for (int pp = 0; pp < NP; ++pp) {
+                                const int j = NP * (j0 + q2) + pp;
+                                bits[q2][pp] =
+                                    (uint64_t)__double_as_longlong(x96_ldexp_rn_general(w0[j], w1[j], w2[j], Eq[q2]));
+                            }
+                    }
+#pragma unroll
+                    for (int q2 = 0; q2 < GQ; ++q2) {
+                        const int jj = j0 + q2;
+                        const int64_t coff = __shfl_sync(0xffffffffu, lcoff, jj);
+                        const int bc = __shfl_sync(0xffffffffu, lexp, jj);
+                        if (!row_ok || bc < 0) continue;
+                        const int64_t off = rowoff + coff;
+                        const bool bad = badrow || bc == 0x7FF;
+                        const double v0 = __longlong_as_double((long long)(bad ? nanb : bits[q2][0]));
+                        if constexpr (CX) {
+                            const double v1 = __longlong_as_double((long long)(bad ? nanb : bits[q2][NP - 1]));
+                            ((double2 *)Cl)[off] = make_double2(v0, v1);
+                        } else {
+                            ((double *)Cl)[off] = v0;
+                        }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int jj = 0; jj < NCOL; ++jj) {
+                    const int64_t coff = __shfl_sync(0xffffffffu, lcoff, jj);
+                    const int bc = __shfl_sync(0xffffffffu, lexp, jj);
+                    if (!row_ok || bc < 0) continue;
+                    const int j = CX ? 2 * jj : jj;
+                    const int64_t off = rowoff + coff;
                     if (CX) ((float2 *)Cl)[off] = make_float2(accf[j], accf[j + 1]);
                     else ((float *)Cl)[off] = accf[j];
                 }

@@ -38,12 +38,23 @@ MGB_HD double x96_bits_to_double(uint64_t b) {
 #endif
 }
 
+// The most significant 32 bits of hi:lo shifted left by c (0 <= c < 32).
+MGB_HD uint32_t x96_shl_funnel(uint32_t lo, uint32_t hi, int c) {
+#if defined(__CUDA_ARCH__)
+    return __funnelshift_l(lo, hi, (unsigned)c);
+#else
+    return (uint32_t)(((((uint64_t)hi << 32) | lo) << c) >> 32);
+#endif
+}
+
 // X * 2^E for the 96-bit two's-complement integer X = w2:w1:w0 (|X| < 2^95),
 // rounded to nearest, ties to even, including subnormal results and overflow
 // to infinity; X = 0 gives +0. Integer operations only: GB300 retires about
 // two FP64 operations per cycle per SM, and a short-K tile writes thousands
-// of outputs per CTA.
-MGB_HD double x96_ldexp_rn(uint32_t w0, uint32_t w1, uint32_t w2, int E) {
+// of outputs per CTA. This is the general routine with a branch per case;
+// the epilogue runs x96_ldexp_bits_fast and comes here only for subnormal
+// results.
+MGB_HD double x96_ldexp_rn_general(uint32_t w0, uint32_t w1, uint32_t w2, int E) {
     const uint64_t neg = w2 >> 31;
     uint64_t lo = ((uint64_t)w1 << 32) | w0;
     uint32_t hi = w2;
@@ -84,6 +95,56 @@ MGB_HD double x96_ldexp_rn(uint32_t w0, uint32_t w1, uint32_t w2, int E) {
     else bits = ((uint64_t)field << 52) + m;  // a carry out of the significand bumps the exponent
     if (bits > 0x7FF0000000000000ull) bits = 0x7FF0000000000000ull;
     return x96_bits_to_double(bits | (neg << 63));
+}
+
+// The bits of x96_ldexp_rn(w0, w1, w2, E) as straight-line code for every
+// result that is not subnormal (normal, infinite, or +0 for X = 0); raises
+// `slow` for a subnormal result, whose bits it does not compute. |X| is
+// normalised so that its leading one is bit 95 (whole words by selects, then
+// a funnel shift), which puts the 53-bit significand, the guard bit and the
+// sticky bits at fixed places. Without branches, the conversions of the
+// columns a thread writes are independent instruction streams that the
+// compiler interleaves.
+MGB_HD uint64_t x96_ldexp_bits_fast(uint32_t w0, uint32_t w1, uint32_t w2, int E, bool &slow) {
+    const uint32_t neg = w2 >> 31, flip = 0u - neg;
+    // |X| = (X ^ flip) + neg over 96 bits
+    uint32_t a0 = w0 ^ flip, a1 = w1 ^ flip, a2 = w2 ^ flip;
+    uint64_t t = (uint64_t)a0 + neg;
+    a0 = (uint32_t)t;
+    t = (uint64_t)a1 + (t >> 32);
+    a1 = (uint32_t)t;
+    a2 += (uint32_t)(t >> 32);
+    int words = 0;  // 32-bit words shifted in from below
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const bool up = a2 == 0;
+        a2 = up ? a1 : a2;
+        a1 = up ? a0 : a1;
+        a0 = up ? 0u : a0;
+        words += up ? 1 : 0;
+    }
+    const int c = x96_clz32(a2) & 31;  // a2 is zero only for X = 0
+    a2 = x96_shl_funnel(a1, a2, c);
+    a1 = x96_shl_funnel(a0, a1, c);
+    a0 <<= c;
+    const int be = 95 - 32 * words - c + E + 1023;  // biased exponent of a normal result
+    const uint64_t sig = ((uint64_t)a2 << 21) | (a1 >> 11);  // bits 95..43
+    const uint32_t guard = (a1 >> 10) & 1u;                 // bit 42
+    const uint32_t sticky = ((a1 & 0x3FFu) | a0) != 0u;      // bits 41..0
+    const uint64_t m = sig + (guard & (sticky | (uint32_t)(sig & 1u)));
+    const uint64_t inf = 0x7FF0000000000000ull;
+    // a carry out of the significand bumps the exponent field
+    uint64_t bits = ((uint64_t)(uint32_t)(be - 1) << 52) + m;
+    bits = (be >= 2047 || bits > inf) ? inf : bits;
+    const bool zero = (w0 | w1 | w2) == 0u;
+    slow = slow || (!zero && be < 1);
+    return zero ? 0ull : bits | ((uint64_t)neg << 63);
+}
+
+MGB_HD double x96_ldexp_rn(uint32_t w0, uint32_t w1, uint32_t w2, int E) {
+    bool slow = false;
+    const uint64_t b = x96_ldexp_bits_fast(w0, w1, w2, E, slow);
+    return slow ? x96_ldexp_rn_general(w0, w1, w2, E) : x96_bits_to_double(b);
 }
 
 }  // namespace mgb

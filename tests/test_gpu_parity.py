@@ -218,3 +218,30 @@ def test_unary_random():
             want = ref.unary(x, ["i", "j", "i", "k"], out)
             tol = 1e-13 if np.dtype(dtype) in (np.float64, np.complex128) else 1e-5
             assert ref.rel_fro(to_np(Y.data), want) <= tol, (dtype, out)
+
+
+def test_ozaki_subnormal_results_correctly_rounded():
+    """Exact-form results below the smallest normal float64 go through the
+    epilogue's general conversion, normal ones through its straight-line
+    path; both must be the correctly rounded value of the exact sum. Integer
+    data scaled by powers of two make the exact sum known: C = (Ai Bi) 2^e
+    with e = -1080 (subnormal) except column 0 (e = -480, normal)."""
+    from fractions import Fraction
+
+    rng = np.random.default_rng(21)
+    ai = rng.integers(-100, 101, size=(8, 16))
+    bi = rng.integers(-100, 101, size=(16, 8))
+    a = np.asfortranarray(ai * 2.0**-540)
+    bscale = np.full(8, 2.0**-540)
+    bscale[0] = 2.0**60
+    b = np.asfortranarray(bi * bscale[None, :])
+    x = ai.astype(object).dot(bi.astype(object))  # exact integers
+    want = np.empty((8, 8))
+    for i in range(8):
+        for j in range(8):
+            e = -480 if j == 0 else -1080
+            want[i, j] = float(Fraction(int(x[i, j])) * Fraction(2) ** e)
+    assert np.any((want != 0) & (np.abs(want) < 2.0**-1022))  # subnormal results present
+    for S in (6, 7):
+        got, _ = run(a, ["i", "k"], b, ["k", "j"], ["i", "j"], "ozaki", S)
+        assert np.array_equal(got.view(np.int64), want.view(np.int64)), S
