@@ -1089,7 +1089,11 @@ def main():
     barrier(ws)
     flops = plan.flops
     value = flops * ws * args.steps / (ms / 1e3) / 1e12
-    launches_per_step = 5  # 2 exponent scans, 2 slicers, 1 tcgen05 GEMM (plus 2 memsets)
+    # kernels of one adaptive step: 2 exponent scans, 2 statistics passes, the
+    # estimate and the choice, 2 slicers, then one tcgen05 GEMM per candidate
+    # slice count (5-8 at 1e-13) and the plain DMMA candidate, of which all but
+    # the chosen one return at once (plus 3 memsets)
+    launches_per_step = 2 + 2 + 1 + 1 + 2 + 4 + 1
 
     # kernel timing for the roofline: phase events around the GEMM launch
     lib.mgb_plan_set_timing(plan.handle, 1)

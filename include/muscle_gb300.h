@@ -143,6 +143,12 @@ int mgb_plan_timing(mgb_plan plan, float *prepass_ms, float *main_ms);
  * 0 = the library's default. Changes the schedule only, never the result.
  * No counterpart in the reference. */
 int mgb_plan_set_band(mgb_plan plan, int32_t band);
+/* *swapped = 1 when an emulated-form plan computes C^T = B^T A^T (A's and
+ * B's roles exchanged inside the library, because A has fewer rows than a
+ * tensor-core tile and B many columns), else 0. Callers pass A and B as
+ * always; the result is the same contraction. Diagnostic only. No
+ * counterpart in the reference. */
+int mgb_plan_operands_swapped(mgb_plan plan, int32_t *swapped);
 /* Target relative Frobenius error (> 0) of an adaptive plan's slice choice;
  * the default 1e-13 is the tolerance Muscle.jl's Float64 results are held
  * to. Set it before executing the plan, not while executions are in flight.

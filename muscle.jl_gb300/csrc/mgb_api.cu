@@ -283,8 +283,12 @@ int mgb_contraction_plan(mgb_plan *plan, const mgb_tensor_desc *a, const mgb_ten
         delete p;
         return st;
     }
-    if (cp.form == MGB_FORM_PLAIN) plain_workspace(cp);
-    else ozaki_setup(cp);
+    if (cp.form == MGB_FORM_PLAIN) {
+        plain_workspace(cp);
+    } else {
+        ozaki_orient(cp);
+        ozaki_setup(cp);
+    }
     if (cp.adaptive && cp.oz_R < 0) {  // no slice count holds K exactly: the plain form
         cp.adaptive = false;
         cp.form = MGB_FORM_PLAIN;
@@ -324,15 +328,15 @@ int mgb_plan_info_get(mgb_plan plan, mgb_plan_info *info) {
         return MGB_OK;
     }
     const ContractionPlan &cp = plan->cp;
-    info->m = cp.M;
-    info->n = cp.N;
+    info->m = cp.swapped ? cp.N : cp.M;  // the caller's A and B
+    info->n = cp.swapped ? cp.M : cp.N;
     info->k = cp.K;
     info->batch = cp.L;
     info->form = cp.form;
     info->slices = (cp.form == MGB_FORM_OZAKI && !cp.adaptive) ? cp.slices : 0;
     info->compute_dtype = cp.compute_dtype;
-    info->permute_a = cp.convert_a;
-    info->permute_b = cp.convert_b;
+    info->permute_a = cp.swapped ? cp.convert_b : cp.convert_a;
+    info->permute_b = cp.swapped ? cp.convert_a : cp.convert_b;
     info->permute_c = 0;
     info->flops = (is_complex(cp.compute_dtype) ? 8.0 : 2.0) * (double)cp.M * (double)cp.N *
                   (double)cp.K * (double)cp.L;
@@ -373,6 +377,7 @@ static int contract_impl(mgb_plan plan, const void *A, const void *B, void *C, v
     if (plan->timing) MGB_CUDA_CHECK(cudaEventRecord(plan->ev[1], s));
     if (cp.K == 0) return launch_fill_zero(C, nc, cp.c.dtype, cp.c, s);  // empty sum
     if (!A || !B) return fail(MGB_ERR_ARGUMENT, "null operand pointer");
+    if (cp.swapped) std::swap(A, B);  // the plan computes C^T = B^T A^T
     if (cp.form == MGB_FORM_PLAIN) return launch_plain_gemm(cp, A, B, C, s);
     return launch_ozaki(cp, A, B, C, workspace, s, plan->timing ? plan->ev[1] : nullptr);
 }
@@ -380,6 +385,13 @@ static int contract_impl(mgb_plan plan, const void *A, const void *B, void *C, v
 int mgb_plan_set_timing(mgb_plan plan, int32_t enable) {
     if (!plan) return fail(MGB_ERR_ARGUMENT, "null plan");
     plan->timing = enable != 0;
+    return MGB_OK;
+}
+
+int mgb_plan_operands_swapped(mgb_plan plan, int32_t *swapped) {
+    if (!plan || !swapped || plan->kind != PlanKind::Contraction)
+        return fail(MGB_ERR_ARGUMENT, "operands_swapped: needs a contraction plan and an output");
+    *swapped = plan->cp.swapped ? 1 : 0;
     return MGB_OK;
 }
 

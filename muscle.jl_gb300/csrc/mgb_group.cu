@@ -72,10 +72,11 @@ static int upload(mgb_group g) {
     for (auto &b : g->buckets) {
         const size_t n = b.members.size();
         std::vector<void *> h(3 * n);
+        const bool sw = b.cp.swapped;  // the plan computes C^T = B^T A^T
         for (size_t i = 0; i < n; ++i) {
             const int m = b.members[i];
-            h[i] = const_cast<void *>(g->A[m]);
-            h[n + i] = const_cast<void *>(g->B[m]);
+            h[i] = const_cast<void *>(sw ? g->B[m] : g->A[m]);
+            h[n + i] = const_cast<void *>(sw ? g->A[m] : g->B[m]);
             h[2 * n + i] = g->C[m];
         }
         MGB_CUDA_CHECK(cudaMemcpy(b.dptr, h.data(), 3 * n * sizeof(void *), cudaMemcpyHostToDevice));

@@ -127,6 +127,11 @@ struct ContractionPlan {
     const void *const *pa = nullptr, *const *pb = nullptr;
     void *const *pc = nullptr;
     int band = 0;          // tensor-core kernel: row tiles per rasterisation band (0: default)
+    // The emulated forms may compute C^T = B^T A^T instead: A and B (their
+    // descriptors, mode strides, extents and pointer tables) are then stored
+    // exchanged, and every entry point passes the caller's B where the plan
+    // says A. Set at plan creation when it fills more of the 128-row tiles.
+    bool swapped = false;
     uint64_t ws_bytes = 0;
     // workspace layout (byte offsets)
     uint64_t ws_a = 0, ws_b = 0, ws_scale_a = 0, ws_scale_b = 0;
@@ -211,4 +216,7 @@ int launch_hadamard(const ModeGroup &g, int ta, int tb, int tc, const void *A, c
 int32_t *device_status_ptr();  // per-device status word
 uint64_t ozaki_workspace(ContractionPlan &p);
 void ozaki_setup(ContractionPlan &p);
+// Emulated forms: exchanges the roles of A and B (see `swapped`) when the
+// tensor-core tiles of C^T = B^T A^T are fewer than those of C = A B.
+void ozaki_orient(ContractionPlan &p);
 }  // namespace mgb

@@ -1387,6 +1387,30 @@ static uint32_t oz_candidates(int64_t k_e, double tol) {
     return m;
 }
 
+// A plan's tensor-core tiles are 128 rows of A by oz_bn embedded columns of
+// B (complex B embeds two columns per column). When A has few rows and B many
+// columns, most of each 128-row tile is empty; C^T = B^T A^T puts the long
+// side on the rows. The exact forms give the same digits and the same exact
+// sums either way (the kept digit pairs and the adaptive error estimate are
+// symmetric in A and B), so only the tile count decides.
+void ozaki_orient(ContractionPlan &p) {
+    if (p.form == MGB_FORM_PLAIN || p.swapped) return;
+    const bool exact = p.form == MGB_FORM_OZAKI, cx = is_complex(p.compute_dtype);
+    const int64_t bn = oz_bn(exact ? p.slices : 3, exact);
+    auto tiles = [&](int64_t rows, int64_t cols) {
+        return ((rows + OZ_BM - 1) / OZ_BM) * (((cx ? 2 : 1) * cols + bn - 1) / bn);
+    };
+    if (tiles(p.N, p.M) >= tiles(p.M, p.N)) return;
+    std::swap(p.a, p.b);
+    std::swap(p.gm, p.gn);
+    for (ModeGroup *g : {&p.gm, &p.gn, &p.gk, &p.gl})
+        for (int i = 0; i < kMaxRank; ++i) std::swap(g->str[0][i], g->str[1][i]);
+    std::swap(p.M, p.N);
+    std::swap(p.convert_a, p.convert_b);
+    std::swap(p.pa, p.pb);
+    p.swapped = true;
+}
+
 void ozaki_setup(ContractionPlan &p) {
     bool cx = is_complex(p.compute_dtype);
     if (p.adaptive) {
@@ -2102,8 +2126,8 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
         const ContractionPlan &p = *it.p;
         if (p.form == MGB_FORM_PLAIN) return fail(MGB_ERR_ARGUMENT, "batch: plain-form plans are not batched");
         if (((uintptr_t)it.ws & 255) != 0) return fail(MGB_ERR_WORKSPACE, "batch: workspace must be 256-byte aligned");
-        fill_prejob(pre[2 * i], p, 0, it.A, it.ws);
-        fill_prejob(pre[2 * i + 1], p, 1, it.B, it.ws);
+        fill_prejob(pre[2 * i], p, 0, p.swapped ? it.B : it.A, it.ws);
+        fill_prejob(pre[2 * i + 1], p, 1, p.swapped ? it.A : it.B, it.ws);
         const bool exact = p.form == MGB_FORM_OZAKI, cx = is_complex(p.compute_dtype);
         if (p.adaptive) {
             OzStatArea a = stat_area(p, it.ws);

@@ -104,6 +104,7 @@ SIGNATURES = {
     "mgb_plan_destroy": (_i32, [_vp]),
     "mgb_plan_set_timing": (_i32, [_vp, _i32]),
     "mgb_plan_set_band": (_i32, [_vp, _i32]),
+    "mgb_plan_operands_swapped": (_i32, [_vp, _P(_i32)]),
     "mgb_plan_timing": (_i32, [_vp, _P(ctypes.c_float), _P(ctypes.c_float)]),
     "mgb_plan_set_tolerance": (_i32, [_vp, ctypes.c_double]),
     "mgb_plan_adaptive_report": (_i32, [_vp, _vp, _vp, _P(AdaptiveReport)]),

@@ -60,6 +60,14 @@ class Plan:
         """True for an OZAKI plan whose slice count is chosen per call."""
         return self.info.form == _lib.FORM_OZAKI and self.info.slices == 0
 
+    @property
+    def operands_swapped(self) -> bool:
+        """True when the library computes C^T = B^T A^T for this plan (an
+        emulated form with few rows in A and many columns in B)."""
+        v = ctypes.c_int32(0)
+        check(_lib.load().mgb_plan_operands_swapped(self.handle, ctypes.byref(v)))
+        return bool(v.value)
+
     def set_tolerance(self, tol: float) -> None:
         """Target relative Frobenius error of an adaptive plan's choice."""
         check(_lib.load().mgb_plan_set_tolerance(self.handle, float(tol)))

@@ -243,3 +243,37 @@ def test_adaptive_plan():
     st, info, _ = _plan(desc(_lib.F64, [0, 1], [40, 50]), desc(_lib.C64, [1, 2], [50, 30]),
                         desc(_lib.C64, [0, 2], [40, 30]), _lib.FORM_PLAIN, 0)
     assert st == 0 and info.workspace_bytes == 0 and info.permute_a == 0
+
+
+def test_emulated_plans_put_the_long_side_on_the_tile_rows():
+    """An emulated plan whose A has few rows and whose B has many columns
+    computes C^T = B^T A^T (the tensor-core tile is 128 rows by 32 or 64
+    embedded columns); plan info keeps the caller's view of M and N, and
+    plain plans keep their orientation."""
+    from muscle_gb300 import _lib
+
+    lib = _lib.load()
+
+    def swapped(dt, m, n, k, form, slices=0):
+        a, b, c = desc(dt, [0, 1], [m, k]), desc(dt, [1, 2], [k, n]), desc(dt, [0, 2], [m, n])
+        da, ka = _lib.make_desc(*a)
+        db, kb = _lib.make_desc(*b)
+        dc, kc = _lib.make_desc(*c)
+        h = ctypes.c_void_p()
+        assert lib.mgb_contraction_plan(ctypes.byref(h), ctypes.byref(da), ctypes.byref(db), ctypes.byref(dc),
+                                        form, slices) == 0
+        v, info = ctypes.c_int32(-1), _lib.PlanInfo()
+        assert lib.mgb_plan_operands_swapped(h, ctypes.byref(v)) == 0
+        assert lib.mgb_plan_info_get(h, ctypes.byref(info)) == 0
+        assert (info.m, info.n, info.k) == (m, n, k)
+        lib.mgb_plan_destroy(h)
+        return v.value
+
+    assert swapped(_lib.F64, 8, 500, 40, _lib.FORM_OZAKI, 6) == 1
+    assert swapped(_lib.C64, 8, 500, 40, _lib.FORM_AUTO, 0) == 1
+    assert swapped(_lib.C32, 20, 900, 64, _lib.FORM_BF16X3) == 1
+    assert swapped(_lib.F64, 500, 8, 40, _lib.FORM_OZAKI, 6) == 0
+    assert swapped(_lib.C64, 48, 48, 4096, _lib.FORM_AUTO, 0) == 0  # square: same tile count
+    assert swapped(_lib.F64, 8, 500, 40, _lib.FORM_PLAIN) == 0
+    v = ctypes.c_int32(0)
+    assert lib.mgb_plan_operands_swapped(None, ctypes.byref(v)) == _lib.ERR_ARGUMENT
