@@ -196,11 +196,14 @@ int mgb_group_update(mgb_group group, const void *const *A,
 int mgb_group_workspace_size(mgb_group group, uint64_t *bytes);
 /* Runs every member on `stream`: the pre-passes of the emulated buckets and
  * the plain buckets, then ONE persistent tensor-core launch per kernel
- * variant over all emulated buckets (each CTA walks tiles of every bucket),
- * then members that run alone. The first execution with a given workspace
- * (and the first after mgb_group_set_tiles) uploads the persistent launch's
- * job table with a synchronous copy; capture the group in a CUDA graph after
- * such a warm-up execution.                                                */
+ * variant over all emulated buckets (each CTA walks tiles of every bucket;
+ * an adaptive bucket has a job in the launch of each candidate slice count,
+ * which works only for the count its device choice names), then the
+ * plain-form fallback of adaptive buckets and members that run alone. The
+ * first execution with a given workspace (and the first after
+ * mgb_group_set_tiles) uploads the persistent launches' job tables with a
+ * synchronous copy; capture the group in a CUDA graph after such a warm-up
+ * execution.                                                               */
 int mgb_group_execute(mgb_group group, void *workspace,
                       uint64_t workspace_bytes, void *stream);
 /* mgb_group_execute in two steps, so that the first can run on several

@@ -120,23 +120,29 @@ static void free_group(mgb_group g) {
 }
 
 // Job tables of the persistent GEMM launches, one per kernel variant
-// (slices, form, real or complex) of the emulated buckets.
+// (slices, form, real or complex) of the emulated buckets. An adaptive
+// bucket has a job in the launch of every candidate slice count, each of
+// which works only when the device chose that count.
 static int build_grouped(mgb_group g, void *workspace) {
     g->retired.insert(g->retired.end(), g->grouped.begin(), g->grouped.end());
     g->grouped.clear();
     g->grouped_ws = nullptr;
     std::map<std::tuple<int, int, int>, std::pair<std::vector<const ContractionPlan *>, std::vector<void *>>> sets;
     for (auto &b : g->buckets) {
-        // plain buckets have no tensor-core part; adaptive ones choose their
-        // slice count on the device and run their own launches
-        if (b.cp.form == MGB_FORM_PLAIN || b.cp.adaptive) continue;
-        auto &e = sets[std::make_tuple(b.cp.slices, b.cp.form, is_complex(b.cp.compute_dtype) ? 1 : 0)];
-        e.first.push_back(&b.cp);
-        e.second.push_back((char *)workspace + b.ws_off);
+        if (b.cp.form == MGB_FORM_PLAIN) continue;  // no tensor-core part
+        const int cx = is_complex(b.cp.compute_dtype) ? 1 : 0;
+        for (int S = 3; S <= 8; ++S) {
+            if (b.cp.adaptive ? !(b.cp.cand_mask & (1u << S)) : S != b.cp.slices) continue;
+            auto &e = sets[std::make_tuple(S, b.cp.form, cx)];
+            e.first.push_back(&b.cp);
+            e.second.push_back((char *)workspace + b.ws_off);
+        }
     }
     for (auto &kv : sets) {
         OzGrouped *x = nullptr;
-        if (int st = ozaki_grouped_create(kv.second.first, kv.second.second, &x)) {
+        const int S = std::get<0>(kv.first);
+        const bool exact = std::get<1>(kv.first) == MGB_FORM_OZAKI, cx = std::get<2>(kv.first) != 0;
+        if (int st = ozaki_grouped_create(kv.second.first, kv.second.second, S, exact, cx, &x)) {
             for (auto *y : g->grouped) ozaki_grouped_destroy(y);  // never launched
             g->grouped.clear();
             return st;
@@ -321,9 +327,11 @@ int mgb_group_finish(mgb_group group, void *workspace, uint64_t workspace_bytes,
         if (int st = build_grouped(group, workspace)) return st;
     for (auto *x : group->grouped)
         if (int st = ozaki_grouped_launch(x, s)) return st;
+    // adaptive buckets whose device choice was the plain form
     for (auto &b : group->buckets)
         if (b.cp.adaptive)
-            if (int st = ozaki_gemm(b.cp, nullptr, nullptr, nullptr, (char *)workspace + b.ws_off, s)) return st;
+            if (int st = ozaki_plain_fallback(b.cp, nullptr, nullptr, nullptr, (char *)workspace + b.ws_off, s))
+                return st;
     const int nb = (int)group->buckets.size(), nu = nb + (int)group->singles.size();
     for (int u = nb; u < nu; ++u)
         if (int st = run_unit(group, u, workspace, s)) return st;

@@ -206,11 +206,18 @@ void ozaki_batch_buffers_destroy(OzBatchBuffers *b);
 int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *buf, cudaStream_t s,
                        int32_t *sel_dev_out, const std::function<int()> &after_prepass,
                        const std::function<int(int S, bool exact, bool cx)> &after_variant);
+// One persistent GEMM launch of kernel variant (S, exact, cx) over plans
+// whose slices lie in `ws`: fixed plans of that variant, and adaptive plans
+// that hold S among their candidates (their jobs work only when the device
+// chose S).
 struct OzGrouped;
-int ozaki_grouped_create(const std::vector<const ContractionPlan *> &plans, const std::vector<void *> &ws,
-                         OzGrouped **out);
+int ozaki_grouped_create(const std::vector<const ContractionPlan *> &plans, const std::vector<void *> &ws, int S,
+                         bool exact, bool cx, OzGrouped **out);
 int ozaki_grouped_launch(const OzGrouped *g, cudaStream_t s);
 void ozaki_grouped_destroy(OzGrouped *g);
+// The plain-form candidate of an adaptive plan after its pre-pass into `ws`
+// (works only when the device chose the plain form; nothing for fixed plans).
+int ozaki_plain_fallback(const ContractionPlan &p, const void *A, const void *B, void *C, void *ws, cudaStream_t s);
 int launch_hadamard(const ModeGroup &g, int ta, int tb, int tc, const void *A, const void *B, void *C,
                     cudaStream_t s);
 int32_t *device_status_ptr();  // per-device status word

@@ -897,7 +897,23 @@ struct OzJobTable {
         local = t - start[lo];
         return jobs[lo];
     }
+    // The first tile after job `hint` that the CTA striding by `grid` from
+    // `first` visits: a skipped job costs one step, not one per tile.
+    __device__ int64_t after_job(int hint, int64_t first, int64_t grid) const {
+        const int64_t e = start[hint + 1];
+        return e + (((first - e) % grid) + grid) % grid;
+    }
 };
+
+// The tile before this CTA's first tile after job `hint` (the tile loop then
+// adds the grid stride): every role of the CTA skips a job of another slice
+// count in one step, and all roles see the same choice, so their tile
+// sequences stay equal.
+template <typename Src>
+__device__ __forceinline__ int64_t skip_job(const Src &src, int hint, int64_t t) {
+    if constexpr (Src::kTable) return src.after_job(hint, blockIdx.x, gridDim.x) - gridDim.x;
+    return t;
+}
 
 // Tile `local` of a job: batch entry, then grouped rasterisation within the
 // entry, so that consecutive tiles walk a band of `band` row tiles across all
@@ -1046,7 +1062,10 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
             for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
                 int64_t local;
                 const OzJob &J = src.job(t, local, hint);
-                if (Src::kTable && J.a.sel && *J.a.sel != S) continue;  // a job of another slice count
+                if (Src::kTable && J.a.sel && *J.a.sel != S) {  // a job of another slice count
+                    t = skip_job(src, hint, t);
+                    continue;
+                }
                 int64_t m0, n0;
                 int l;
                 oz_tile(J, local, BN, m0, n0, l);
@@ -1083,7 +1102,10 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
             for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
                 int64_t local;
                 const OzJob &J = src.job(t, local, hint);
-                if (Src::kTable && J.a.sel && *J.a.sel != S) continue;  // a job of another slice count
+                if (Src::kTable && J.a.sel && *J.a.sel != S) {  // a job of another slice count
+                    t = skip_job(src, hint, t);
+                    continue;
+                }
                 const int nkb = J.a.nkb, kcb = J.a.kcb;
                 for (int c0 = 0; c0 < nkb && ok; c0 += kcb, ++C) {
                     const uint32_t bank = C & 1u;
@@ -1132,7 +1154,10 @@ __device__ __forceinline__ void oz_gemm_body(const Src &src) {
         for (int64_t t = blockIdx.x; t < T && ok; t += gridDim.x) {
             int64_t local;
             const OzJob &J = src.job(t, local, hint);
-            if (Src::kTable && J.a.sel && *J.a.sel != S) continue;  // a job of another slice count
+            if (Src::kTable && J.a.sel && *J.a.sel != S) {  // a job of another slice count
+                t = skip_job(src, hint, t);
+                continue;
+            }
             const OzGemmArgs &args = J.a;
             int64_t m0, n0;
             int l;
@@ -1824,24 +1849,29 @@ struct OzGrouped {
     int64_t *start = nullptr;  // device [njobs + 1]
 };
 
-int ozaki_grouped_create(const std::vector<const ContractionPlan *> &plans, const std::vector<void *> &ws,
-                         OzGrouped **out) {
+int ozaki_grouped_create(const std::vector<const ContractionPlan *> &plans, const std::vector<void *> &ws, int S,
+                         bool exact, bool cx, OzGrouped **out) {
     *out = nullptr;
     if (plans.empty()) return fail(MGB_ERR_ARGUMENT, "grouped GEMM: no plans");
     auto *g = new OzGrouped();
-    g->S = plans[0]->slices;
-    g->exact = plans[0]->form == MGB_FORM_OZAKI;
-    g->cx = is_complex(plans[0]->compute_dtype);
+    g->S = S;
+    g->exact = exact;
+    g->cx = cx;
     std::vector<OzJob> host(plans.size());
     std::vector<int64_t> start(plans.size() + 1, 0);
     for (size_t i = 0; i < plans.size(); ++i) {
         const ContractionPlan &p = *plans[i];
-        if (p.slices != g->S || (p.form == MGB_FORM_OZAKI) != g->exact || is_complex(p.compute_dtype) != g->cx) {
+        const bool variant_ok = (p.form == MGB_FORM_OZAKI) == exact && is_complex(p.compute_dtype) == cx &&
+                                (p.adaptive ? exact && (p.cand_mask & (1u << S)) != 0 : p.slices == S);
+        if (!variant_ok) {
             delete g;
             return fail(MGB_ERR_ARGUMENT, "grouped GEMM: plans of different kernel variants");
         }
         int64_t t = 0;
-        if (int st = ozaki_job(p, nullptr, ws[i], host[i], t)) {
+        // an adaptive plan's job works only when its device choice is S
+        const int st = p.adaptive ? ozaki_job(p, nullptr, ws[i], host[i], t, S, &stat_area(p, ws[i]).st->sel)
+                                  : ozaki_job(p, nullptr, ws[i], host[i], t);
+        if (st) {
             delete g;
             return st;
         }
@@ -2063,7 +2093,8 @@ static void fill_prejob(PreJob &J, const ContractionPlan &p, int t, const void *
     std::memset(&J, 0, sizeof(J));
     const bool cx = is_complex(p.compute_dtype), exact = p.form == MGB_FORM_OZAKI;
     uint8_t *w = (uint8_t *)ws;
-    J.g.ptrs = nullptr;
+    // one operand, or (X null) the plan's per-batch-entry pointer table
+    J.g.ptrs = X ? nullptr : (t == 0 ? p.pa : p.pb);
     J.g.gr = t == 0 ? p.gm : p.gn;
     J.g.gk = p.gk;
     J.g.gl = p.gl;
@@ -2109,6 +2140,111 @@ static void fill_prejob(PreJob &J, const ContractionPlan &p, int t, const void *
     J.tiles[PRE_SLICE] = ((R + 31) / 32) * ((K + OZ_SLICE_KT - 1) / OZ_SLICE_KT) * L;
 }
 
+// The chooser's job for an adaptive plan whose statistics lie in `ws`.
+static ChooseJob choose_job(const ContractionPlan &p, void *ws) {
+    OzStatArea a = stat_area(p, ws);
+    ChooseJob c;
+    c.st = a.st;
+    c.qa = a.qa;
+    c.qb = a.qb;
+    c.pa = a.pa;
+    c.pb = a.pb;
+    c.K = p.K;
+    c.L = p.L;
+    c.cand = p.cand_mask;
+    c.cx = is_complex(p.compute_dtype) ? 1 : 0;
+    c.tol = p.tol;
+    c.margin = 1.0 + 2.0 / std::sqrt((double)std::max<int64_t>(p.M * p.N * p.L, 1));
+    return c;
+}
+
+// Pre-pass tables of emulated items: two operand jobs per item (operands
+// given by pointer, or, when null, by the plan's pointer tables), one
+// chooser job per adaptive item.
+static int pre_tables(const std::vector<OzBatchItem> &items, std::vector<PreJob> &pre, std::vector<ChooseJob> &choose) {
+    pre.assign(2 * items.size(), PreJob{});
+    choose.clear();
+    for (size_t i = 0; i < items.size(); ++i) {
+        const OzBatchItem &it = items[i];
+        const ContractionPlan &p = *it.p;
+        if (p.form == MGB_FORM_PLAIN) return fail(MGB_ERR_ARGUMENT, "batch: plain-form plans are not batched");
+        if (((uintptr_t)it.ws & 255) != 0) return fail(MGB_ERR_WORKSPACE, "batch: workspace must be 256-byte aligned");
+        fill_prejob(pre[2 * i], p, 0, p.swapped ? it.B : it.A, it.ws);
+        fill_prejob(pre[2 * i + 1], p, 1, p.swapped ? it.A : it.B, it.ws);
+        if (p.adaptive) choose.push_back(choose_job(p, it.ws));
+    }
+    return MGB_OK;
+}
+
+// Byte offsets of the pre-pass tables in one device area: [pre jobs]
+// [block starts of each phase][chooser jobs][their estimate blocks' starts].
+struct PreLayout {
+    size_t o_pre = 0, o_pst = 0, o_ch = 0, o_cs = 0, end = 0;
+    int64_t blocks[PRE_PHASES] = {};
+    int64_t est_blocks = 0;
+};
+static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+static PreLayout pre_layout(const std::vector<PreJob> &pre, const std::vector<ChooseJob> &choose, size_t base) {
+    PreLayout L;
+    size_t off = base;
+    L.o_pre = off;
+    off = al256(off + pre.size() * sizeof(PreJob));
+    L.o_pst = off;
+    off = al256(off + PRE_PHASES * (pre.size() + 1) * sizeof(int64_t));
+    L.o_ch = off;
+    off = al256(off + choose.size() * sizeof(ChooseJob));
+    L.o_cs = off;
+    off = al256(off + (choose.size() + 1) * sizeof(int64_t));
+    L.end = off;
+    return L;
+}
+// Writes the tables at their offsets of host area `h` and fills the block counts.
+static void pre_write(PreLayout &L, const std::vector<PreJob> &pre, const std::vector<ChooseJob> &choose, uint8_t *h) {
+    std::memcpy(h + L.o_pre, pre.data(), pre.size() * sizeof(PreJob));
+    int64_t *pst = (int64_t *)(h + L.o_pst);
+    for (int ph = 0; ph < PRE_PHASES; ++ph) {
+        int64_t *st = pst + ph * (pre.size() + 1);
+        st[0] = 0;
+        for (size_t j = 0; j < pre.size(); ++j) st[j + 1] = st[j] + pre[j].tiles[ph];
+        L.blocks[ph] = st[pre.size()];
+    }
+    std::memcpy(h + L.o_ch, choose.data(), choose.size() * sizeof(ChooseJob));
+    int64_t *cst = (int64_t *)(h + L.o_cs);
+    cst[0] = 0;
+    for (size_t j = 0; j < choose.size(); ++j) cst[j + 1] = cst[j] + oz_est_blocks(choose[j].K) * choose[j].L;
+    L.est_blocks = cst[choose.size()];
+}
+// Every pre-pass phase over the tables at device area `d`: one launch per
+// phase, the estimate and the choice before the slicing.
+static int pre_launch(const PreLayout &L, size_t npre, size_t nch, const uint8_t *d, cudaStream_t s) {
+    const PreJob *dpre = (const PreJob *)(d + L.o_pre);
+    for (int ph = 0; ph < PRE_PHASES; ++ph) {
+        if (ph == PRE_SLICE && nch > 0) {
+            if (L.est_blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "batch: estimate grid too large");
+            if (L.est_blocks > 0) {
+                k_oz_est_multi<<<(unsigned)L.est_blocks, 256, 0, s>>>((const ChooseJob *)(d + L.o_ch),
+                                                                      (const int64_t *)(d + L.o_cs), (int)nch);
+                MGB_CUDA_CHECK(cudaGetLastError());
+            }
+            k_oz_choose_multi<<<((int)nch + 127) / 128, 128, 0, s>>>((const ChooseJob *)(d + L.o_ch), (int)nch);
+            MGB_CUDA_CHECK(cudaGetLastError());
+        }
+        if (L.blocks[ph] == 0) continue;
+        if (L.blocks[ph] > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "batch: pre-pass grid too large");
+        k_oz_pre_multi<<<(unsigned)L.blocks[ph], 256, 0, s>>>(dpre, (const int64_t *)(d + L.o_pst) + ph * (npre + 1),
+                                                              (int)npre, ph);
+        MGB_CUDA_CHECK(cudaGetLastError());
+    }
+    return MGB_OK;
+}
+
+// The plain-form candidate of an adaptive plan (runs only when the device
+// chose no slice count), after its pre-pass into `ws`.
+int ozaki_plain_fallback(const ContractionPlan &p, const void *A, const void *B, void *C, void *ws, cudaStream_t s) {
+    if (!p.adaptive) return MGB_OK;
+    return launch_plain_gemm(p, A, B, C, s, &stat_area(p, ws).st->sel);
+}
+
 int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *buf, cudaStream_t s,
                        int32_t *sel_dev_out, const std::function<int()> &after_prepass,
                        const std::function<int(int S, bool exact, bool cx)> &after_variant) {
@@ -2117,33 +2253,17 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
     int32_t *status = device_status_ptr();
     if (!status) return fail(MGB_ERR_CUDA, "device status word unavailable");
     // ---- host tables
-    std::vector<PreJob> pre(2 * n);
+    std::vector<PreJob> pre;
     std::vector<ChooseJob> choose;
+    if (int st = pre_tables(items, pre, choose)) return st;
     // GEMM jobs per variant: key (S, exact, cx) ordered cheapest first
     std::map<std::tuple<int, int, int>, std::vector<OzJob>> gem;
     for (int i = 0; i < n; ++i) {
         const OzBatchItem &it = items[i];
         const ContractionPlan &p = *it.p;
-        if (p.form == MGB_FORM_PLAIN) return fail(MGB_ERR_ARGUMENT, "batch: plain-form plans are not batched");
-        if (((uintptr_t)it.ws & 255) != 0) return fail(MGB_ERR_WORKSPACE, "batch: workspace must be 256-byte aligned");
-        fill_prejob(pre[2 * i], p, 0, p.swapped ? it.B : it.A, it.ws);
-        fill_prejob(pre[2 * i + 1], p, 1, p.swapped ? it.A : it.B, it.ws);
         const bool exact = p.form == MGB_FORM_OZAKI, cx = is_complex(p.compute_dtype);
         if (p.adaptive) {
             OzStatArea a = stat_area(p, it.ws);
-            ChooseJob c;
-            c.st = a.st;
-            c.qa = a.qa;
-            c.qb = a.qb;
-            c.pa = a.pa;
-            c.pb = a.pb;
-            c.K = p.K;
-            c.L = p.L;
-            c.cand = p.cand_mask;
-            c.cx = cx ? 1 : 0;
-            c.tol = p.tol;
-            c.margin = 1.0 + 2.0 / std::sqrt((double)std::max<int64_t>(p.M * p.N * p.L, 1));
-            choose.push_back(c);
             for (int S = 3; S <= 8; ++S) {
                 if (!(p.cand_mask & (1u << S))) continue;
                 OzJob job;
@@ -2158,18 +2278,11 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
             gem[std::make_tuple(exact ? p.slices : 3, exact ? 1 : 0, cx ? 1 : 0)].push_back(job);
         }
     }
-    // ---- one staging area: [pre jobs][pre starts x 4 phases][choose jobs, their estimate blocks' starts]
-    //      [per item: fixed slice count, address of its slice count][per variant: jobs, starts]
-    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    size_t off = 0;
-    const size_t o_pre = off;
-    off = al(off + pre.size() * sizeof(PreJob));
-    const size_t o_pst = off;
-    off = al(off + PRE_PHASES * (pre.size() + 1) * sizeof(int64_t));
-    const size_t o_ch = off;
-    off = al(off + choose.size() * sizeof(ChooseJob));
-    const size_t o_cs = off;
-    off = al(off + (choose.size() + 1) * sizeof(int64_t));
+    // ---- one staging area: [pre-pass tables][per item: fixed slice count,
+    //      address of its slice count][per variant: jobs, starts]
+    auto al = al256;
+    PreLayout PL = pre_layout(pre, choose, 0);
+    size_t off = PL.end;
     // per item: the address of its slice count (adaptive: the choice; else
     // the fixed count stored here)
     const size_t o_fix = off;
@@ -2185,20 +2298,7 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
     }
     if (int st = batch_reserve(buf, off)) return st;
     uint8_t *h = buf->host, *d = buf->dev;
-    std::memcpy(h + o_pre, pre.data(), pre.size() * sizeof(PreJob));
-    int64_t *pst = (int64_t *)(h + o_pst);
-    int64_t blocks[PRE_PHASES];
-    for (int ph = 0; ph < PRE_PHASES; ++ph) {
-        int64_t *st = pst + ph * (pre.size() + 1);
-        st[0] = 0;
-        for (size_t j = 0; j < pre.size(); ++j) st[j + 1] = st[j] + pre[j].tiles[ph];
-        blocks[ph] = st[pre.size()];
-    }
-    std::memcpy(h + o_ch, choose.data(), choose.size() * sizeof(ChooseJob));
-    int64_t *cst = (int64_t *)(h + o_cs);
-    cst[0] = 0;
-    for (size_t j = 0; j < choose.size(); ++j) cst[j + 1] = cst[j] + oz_est_blocks(choose[j].K) * choose[j].L;
-    const int64_t est_blocks = cst[choose.size()];
+    pre_write(PL, pre, choose, h);
     for (int i = 0; i < n; ++i) {
         const ContractionPlan &p = *items[i].p;
         ((int32_t *)(h + o_fix))[i] = p.form == MGB_FORM_OZAKI ? p.slices : 3;
@@ -2219,25 +2319,7 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
     MGB_CUDA_CHECK(cudaMemcpyAsync(d, h, off, cudaMemcpyHostToDevice, s));
     MGB_CUDA_CHECK(cudaEventRecord(buf->staged, s));
     // ---- pre-pass phases
-    const PreJob *dpre = (const PreJob *)(d + o_pre);
-    for (int ph = 0; ph < PRE_PHASES; ++ph) {
-        if (ph == PRE_SLICE && !choose.empty()) {
-            if (est_blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "batch: estimate grid too large");
-            if (est_blocks > 0) {
-                k_oz_est_multi<<<(unsigned)est_blocks, 256, 0, s>>>((const ChooseJob *)(d + o_ch),
-                                                                    (const int64_t *)(d + o_cs), (int)choose.size());
-                MGB_CUDA_CHECK(cudaGetLastError());
-            }
-            const int nc = (int)choose.size();
-            k_oz_choose_multi<<<(nc + 127) / 128, 128, 0, s>>>((const ChooseJob *)(d + o_ch), nc);
-            MGB_CUDA_CHECK(cudaGetLastError());
-        }
-        if (blocks[ph] == 0) continue;
-        if (blocks[ph] > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "batch: pre-pass grid too large");
-        k_oz_pre_multi<<<(unsigned)blocks[ph], 256, 0, s>>>(dpre, (const int64_t *)(d + o_pst) + ph * (pre.size() + 1),
-                                                            (int)pre.size(), ph);
-        MGB_CUDA_CHECK(cudaGetLastError());
-    }
+    if (int st = pre_launch(PL, pre.size(), choose.size(), d, s)) return st;
     // every item's slice count (its fixed count, or the device's choice; 0 = plain)
     if (sel_dev_out) {
         k_gather_sel<<<(n + 255) / 256, 256, 0, s>>>((const int32_t *const *)(d + o_sp), sel_dev_out, n);
