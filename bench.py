@@ -59,15 +59,17 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
     ap.add_argument("--workload", default="precision",
                     choices=["precision", "peps", "serve", "config2", "kernel", "permute", "hadamard", "unary", "fp64",
-                             "blocks"],
+                             "blocks", "shortk"],
                     help="precision: the headline line; peps / serve: batching and serving forms; config2: "
                          "plain shapes that permute; kernel / permute: one contraction of the precision "
                          "workload at --n / the permutation of A(a,b,c,d,e) with e = --perm-e (profiling cases); "
                          "hadamard / unary: broadcast product / partial sums of a 4.3 GB array; blocks: the "
-                         "precision workload at --n/2 contracted whole and block by block")
+                         "precision workload at --n/2 contracted whole and block by block; shortk: 8192 x --k x 8192 "
+                         "(GEMM epilogue rate)")
     ap.add_argument("--form", default="ozaki", help="form of --workload kernel")
     ap.add_argument("--band", type=int, default=0, help="rasterisation band of --workload kernel (0: default)")
     ap.add_argument("--perm-e", type=int, default=32, help="extent of label e in --workload permute")
+    ap.add_argument("--k", type=int, default=8, help="contracted extent of --workload shortk")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="per offered rate in the serving sweep")
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--serve-pool", type=int, default=4096, help="distinct requests of the serving workload")
@@ -728,6 +730,46 @@ def kernel_case(dev, n, form, slices, steps, warmup, band=0):
             "tflops_alg": p.flops / ((statistics.mean(pre) + ms) / 1e3) / 1e12, "status": m.device_status(dev)}
 
 
+def shortk_case(dev, k, steps, warmup, n=8192, slices=6):
+    """C(i,j) = A(i,k) B(k,j), ComplexF64, M = N = n and a short contracted
+    extent k: tiles with one or few k blocks, whose time is the GEMM
+    epilogue's (profiling case); fixed slice count, phase timing from the plan."""
+    import ctypes
+
+    import torch
+
+    import muscle_gb300 as m
+    from muscle_gb300 import _lib
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    A = m.empty_colmajor([n, k], torch.complex128, dev)
+    A.copy_(torch.randn(n, k, dtype=torch.complex128, device=dev, generator=g))
+    B = m.empty_colmajor([k, n], torch.complex128, dev)
+    B.copy_(torch.randn(k, n, dtype=torch.complex128, device=dev, generator=g))
+    C = m.empty_colmajor([n, n], torch.complex128, dev)
+    I = [m.Index(x) for x in ("i", "k", "j")]
+    p = m.contraction_plan(A, [I[0], I[1]], B, [I[1], I[2]], C, [I[0], I[2]], "ozaki", slices)
+    ws = torch.empty(max(p.workspace_bytes, 1), dtype=torch.uint8, device=dev)
+    lib = _lib.load()
+    st = torch.cuda.current_stream(dev).cuda_stream
+    lib.mgb_plan_set_timing(p.handle, 1)
+    pre, main = [], []
+    for r in range(warmup + steps):
+        _lib.check(lib.mgb_contract(p.handle, A.data_ptr(), B.data_ptr(), C.data_ptr(), ws.data_ptr(), ws.numel(),
+                                    st), lib)
+        fp, fm = ctypes.c_float(), ctypes.c_float()
+        _lib.check(lib.mgb_plan_timing(p.handle, ctypes.byref(fp), ctypes.byref(fm)), lib)
+        if r >= warmup:
+            pre.append(fp.value)
+            main.append(fm.value)
+    gemm = statistics.median(main)
+    tiles = (n // 128) * (2 * n // 32)
+    return {"n": n, "k": k, "slices": slices, "tiles": tiles, "prepass_ms": statistics.median(pre), "gemm_ms": gemm,
+            "gemm_cycles_per_tile_per_sm_at_2070mhz": gemm * 1e-3 * 2.07e9 * 152 / tiles,
+            "status": m.device_status(dev)}
+
+
 def permute_case(dev, e, steps, warmup, dtype="c64"):
     """Permutation of A(a,b,c,d,e) = 64x96x64x48xe ComplexF64 (or Float64) to
     (b,d,a,c,e), the reordering the host backend stages for the permuting
@@ -890,6 +932,9 @@ def main():
         elif args.workload == "kernel":
             res = kernel_case(dev, args.n, args.form, args.slices, args.steps, args.warmup, args.band)
             metric = "one contraction of the precision workload (profiling case)"
+        elif args.workload == "shortk":
+            res = shortk_case(dev, args.k, args.steps, args.warmup)
+            metric = "short-K contraction: GEMM epilogue rate (profiling case)"
         elif args.workload == "permute":
             res = {d: permute_case(dev, args.perm_e, args.steps, args.warmup, d) for d in ("c64", "f64")}
             metric = "permutation kernel GB/s (profiling case)"
