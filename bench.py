@@ -1032,16 +1032,17 @@ def main():
     # End to end through the public API with host buffers: every step copies
     # its inputs from pinned host memory, contracts, and copies the result back
     # (byte-for-byte copies of the column-major arrays as flat buffers).
-    # Steps rotate over three device buffer sets. One copy stream carries both
+    # Steps rotate over four device buffer sets. One copy stream carries both
     # directions in order: once step i has computed, its result goes back and
-    # then step i + 3's inputs come in, while steps i + 1 and i + 2 compute
+    # then step i + 4's inputs come in, while the next three steps compute
     # (about 15 ms of copies at ~200 GB/s against about 78 ms of compute per
-    # step). Single host copies on the shared GB300 hosts sometimes took 40-70
-    # ms instead of 5-10; two steps of slack keep such a copy off the
-    # critical path. This runs before the device-timed loop and its clock
+    # step). On the shared GB300 hosts, copies were slowed periodically (a
+    # result copy of ~70 ms followed by an input copy of ~130 ms about every
+    # half second, instead of 5 and 10 ms); three steps of slack keep such a
+    # pair off the critical path. This runs before the device-timed loop and its clock
     # sampler: host copies in the first few hundred milliseconds after
     # nvidia-smi started also ran at a fraction of their usual rate.
-    NSET = 3
+    NSET = 4
     cset = []
     for _ in range(NSET):
         af = torch.empty(a_f.numel(), dtype=torch.complex128, device=dev)
@@ -1237,8 +1238,8 @@ def main():
             "speedup_vs_native": value / native,
             "e2e": {"value": e2e, "unit": "TFLOP/s", "ms_per_step": e2e_ms / e2e_steps, "steps": e2e_steps,
                     "h2d_bytes_per_step": A.numel() * 16 + B.numel() * 16, "d2h_bytes_per_step": C.numel() * 16,
-                    "pipelined": "result of step i, then inputs of step i + 3, on one copy stream while steps i + 1 "
-                                 "and i + 2 compute (three buffer sets)",
+                    "pipelined": "result of step i, then inputs of step i + 4, on one copy stream while the next "
+                                 "three steps compute (four buffer sets)",
                     "result_matches_device_run": e2e_ok, "phases": e2e_phases},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": achieved / bf16_peak, "traffic": traffic, "peak_kind": f"bf16 dense burst ({peak_kind})",

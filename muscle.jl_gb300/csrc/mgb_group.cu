@@ -139,6 +139,23 @@ static int build_grouped(mgb_group g, void *workspace) {
         }
     }
     for (auto &kv : sets) {
+        // longest tiles first: each CTA then ends its walk on short tiles,
+        // which even out the CTAs' finishing times
+        {
+            auto &pl = kv.second.first;
+            auto &wl = kv.second.second;
+            std::vector<size_t> ord(pl.size());
+            for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+            std::stable_sort(ord.begin(), ord.end(), [&](size_t u, size_t v) { return pl[u]->k_e > pl[v]->k_e; });
+            std::vector<const ContractionPlan *> p2;
+            std::vector<void *> w2;
+            for (size_t i : ord) {
+                p2.push_back(pl[i]);
+                w2.push_back(wl[i]);
+            }
+            pl.swap(p2);
+            wl.swap(w2);
+        }
         OzGrouped *x = nullptr;
         const int S = std::get<0>(kv.first);
         const bool exact = std::get<1>(kv.first) == MGB_FORM_OZAKI, cx = std::get<2>(kv.first) != 0;

@@ -2278,6 +2278,11 @@ int ozaki_batch_launch(const std::vector<OzBatchItem> &items, OzBatchBuffers *bu
             gem[std::make_tuple(exact ? p.slices : 3, exact ? 1 : 0, cx ? 1 : 0)].push_back(job);
         }
     }
+    // longest tiles first in every variant's launch: each CTA ends its walk
+    // on short tiles, which even out the CTAs' finishing times
+    for (auto &kv : gem)
+        std::stable_sort(kv.second.begin(), kv.second.end(),
+                         [](const OzJob &u, const OzJob &v) { return u.a.nkb > v.a.nkb; });
     // ---- one staging area: [pre-pass tables][per item: fixed slice count,
     //      address of its slice count][per variant: jobs, starts]
     auto al = al256;
