@@ -2029,6 +2029,51 @@ __global__ void __launch_bounds__(256, 3) k_oz_pre_multi(const PreJob *__restric
 }
 
 // dst[i] = *src[i]: every item's slice count after the choice
+// The last job of a table whose first block is <= b.
+__device__ __forceinline__ int multi_job(const int64_t *__restrict__ start, int njobs, int64_t b) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (start[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Exponent scan over a table of operand jobs of one element type: the same
+// tile routine, shared memory and occupancy as the single-plan scan, for
+// many operands in one launch (no launch per operand, one tail for all).
+template <typename T>
+__global__ void __launch_bounds__(256, 4) k_oz_scale_multi(const PreJob *__restrict__ jobs,
+                                                        const int64_t *__restrict__ start, int njobs) {
+    __shared__ ScaleSmem sm;
+    const int j = multi_job(start, njobs, blockIdx.x);
+    const PreJob &J = jobs[j];
+    const int64_t local = blockIdx.x - start[j];
+    const int64_t per_l = J.tiles[PRE_SCALE] / max(J.L, 1);
+    const int64_t l = local / per_l;
+    oz_scale_tile<T>((const T *)J.X, J.g, J.exps, J.emax, J.part, local - l * per_l, l, sm);
+}
+
+// Slicing over a table of operand jobs of one element type, embedding and
+// form, as the single-plan slicer does it.
+template <typename T, int MODE, bool BF3>
+__global__ void __launch_bounds__(256, 4) k_oz_slice_multi(const PreJob *__restrict__ jobs,
+                                                        const int64_t *__restrict__ start, int njobs) {
+    __shared__ SliceSmemOf<T, MODE> sm;
+    const int j = multi_job(start, njobs, blockIdx.x);
+    const PreJob &J = jobs[j];
+    int S = J.S;
+    if (J.sel) {
+        S = *J.sel;
+        if (S == 0) return;  // the plain form will run this contraction
+    }
+    const int64_t local = blockIdx.x - start[j];
+    const int64_t per_l = J.tiles[PRE_SLICE] / max(J.L, 1);
+    const int64_t l = local / per_l;
+    oz_slice_tile<T, MODE, BF3>((const T *)J.X, J.g, J.exps, S, J.out, J.rows_e, J.kw, local - l * per_l, l, sm);
+}
+
 __global__ void k_gather_sel(const int32_t *const *__restrict__ src, int32_t *__restrict__ dst, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dst[i] = *src[i];
@@ -2173,15 +2218,27 @@ static int pre_tables(const std::vector<OzBatchItem> &items, std::vector<PreJob>
         fill_prejob(pre[2 * i + 1], p, 1, p.swapped ? it.A : it.B, it.ws);
         if (p.adaptive) choose.push_back(choose_job(p, it.ws));
     }
+    // operand jobs of one (form, element type, embedding) lie together: the
+    // scan and the slicer run one launch per such segment
+    std::stable_sort(pre.begin(), pre.end(), [](const PreJob &u, const PreJob &v) {
+        return std::make_tuple(u.bf3, u.dtype, u.mode) < std::make_tuple(v.bf3, v.dtype, v.mode);
+    });
     return MGB_OK;
 }
 
 // Byte offsets of the pre-pass tables in one device area: [pre jobs]
 // [block starts of each phase][chooser jobs][their estimate blocks' starts].
+struct PreSegment {
+    int first = 0, count = 0;  // operand jobs [first, first + count)
+    int32_t bf3 = 0, dtype = 0, mode = 0;
+    size_t o_scale = 0, o_slice = 0;  // their block starts of the scan and the slicer
+    int64_t scale_blocks = 0, slice_blocks = 0;
+};
 struct PreLayout {
     size_t o_pre = 0, o_pst = 0, o_ch = 0, o_cs = 0, end = 0;
     int64_t blocks[PRE_PHASES] = {};
     int64_t est_blocks = 0;
+    std::vector<PreSegment> seg;  // runs of jobs with one (form, element type, embedding)
 };
 static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 static PreLayout pre_layout(const std::vector<PreJob> &pre, const std::vector<ChooseJob> &choose, size_t base) {
@@ -2195,6 +2252,20 @@ static PreLayout pre_layout(const std::vector<PreJob> &pre, const std::vector<Ch
     off = al256(off + choose.size() * sizeof(ChooseJob));
     L.o_cs = off;
     off = al256(off + (choose.size() + 1) * sizeof(int64_t));
+    for (size_t j = 0; j < pre.size();) {
+        PreSegment g;
+        g.first = (int)j;
+        g.bf3 = pre[j].bf3;
+        g.dtype = pre[j].dtype;
+        g.mode = pre[j].mode;
+        while (j < pre.size() && pre[j].bf3 == g.bf3 && pre[j].dtype == g.dtype && pre[j].mode == g.mode) ++j;
+        g.count = (int)j - g.first;
+        g.o_scale = off;
+        off = al256(off + (g.count + 1) * sizeof(int64_t));
+        g.o_slice = off;
+        off = al256(off + (g.count + 1) * sizeof(int64_t));
+        L.seg.push_back(g);
+    }
     L.end = off;
     return L;
 }
@@ -2208,14 +2279,68 @@ static void pre_write(PreLayout &L, const std::vector<PreJob> &pre, const std::v
         for (size_t j = 0; j < pre.size(); ++j) st[j + 1] = st[j] + pre[j].tiles[ph];
         L.blocks[ph] = st[pre.size()];
     }
+    for (PreSegment &g : L.seg) {
+        int64_t *a = (int64_t *)(h + g.o_scale), *b = (int64_t *)(h + g.o_slice);
+        a[0] = b[0] = 0;
+        for (int j = 0; j < g.count; ++j) {
+            a[j + 1] = a[j] + pre[g.first + j].tiles[PRE_SCALE];
+            b[j + 1] = b[j] + pre[g.first + j].tiles[PRE_SLICE];
+        }
+        g.scale_blocks = a[g.count];
+        g.slice_blocks = b[g.count];
+    }
     std::memcpy(h + L.o_ch, choose.data(), choose.size() * sizeof(ChooseJob));
     int64_t *cst = (int64_t *)(h + L.o_cs);
     cst[0] = 0;
     for (size_t j = 0; j < choose.size(); ++j) cst[j + 1] = cst[j] + oz_est_blocks(choose[j].K) * choose[j].L;
     L.est_blocks = cst[choose.size()];
 }
-// Every pre-pass phase over the tables at device area `d`: one launch per
-// phase, the estimate and the choice before the slicing.
+// One typed launch of phase `ph` (scan or slicing) over segment `g`.
+static int seg_launch(const PreSegment &g, int ph, const PreJob *dpre, const uint8_t *d, cudaStream_t s) {
+    const int64_t blocks = ph == PRE_SCALE ? g.scale_blocks : g.slice_blocks;
+    if (blocks == 0) return MGB_OK;
+    if (blocks > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "batch: pre-pass grid too large");
+    const PreJob *jobs = dpre + g.first;
+    const int64_t *st = (const int64_t *)(d + (ph == PRE_SCALE ? g.o_scale : g.o_slice));
+    const unsigned nb = (unsigned)blocks;
+    if (ph == PRE_SCALE) {
+        switch (g.dtype) {
+        case MGB_F64: k_oz_scale_multi<double><<<nb, 256, 0, s>>>(jobs, st, g.count); break;
+        case MGB_C64: k_oz_scale_multi<double2><<<nb, 256, 0, s>>>(jobs, st, g.count); break;
+        case MGB_F32: k_oz_scale_multi<float><<<nb, 256, 0, s>>>(jobs, st, g.count); break;
+        default: k_oz_scale_multi<float2><<<nb, 256, 0, s>>>(jobs, st, g.count); break;
+        }
+    } else {
+#define MGB_SLICE_MULTI(T, MODE, BF3) k_oz_slice_multi<T, MODE, BF3><<<nb, 256, 0, s>>>(jobs, st, g.count)
+        auto by_mode = [&](auto tag, bool bf3) {
+            using T = typename std::remove_pointer<decltype(tag)>::type;
+            if (bf3) {
+                if constexpr (std::is_same<T, float>::value || std::is_same<T, float2>::value) {
+                    if (g.mode == MODE_CA) MGB_SLICE_MULTI(T, MODE_CA, true);
+                    else if (g.mode == MODE_CB) MGB_SLICE_MULTI(T, MODE_CB, true);
+                    else if constexpr (!OzIn<T>::cx) MGB_SLICE_MULTI(T, MODE_REAL, true);
+                }
+            } else {
+                if (g.mode == MODE_CA) MGB_SLICE_MULTI(T, MODE_CA, false);
+                else if (g.mode == MODE_CB) MGB_SLICE_MULTI(T, MODE_CB, false);
+                else if constexpr (!OzIn<T>::cx) MGB_SLICE_MULTI(T, MODE_REAL, false);
+            }
+        };
+#undef MGB_SLICE_MULTI
+        switch (g.dtype) {
+        case MGB_F64: by_mode((double *)nullptr, g.bf3 != 0); break;
+        case MGB_C64: by_mode((double2 *)nullptr, g.bf3 != 0); break;
+        case MGB_F32: by_mode((float *)nullptr, g.bf3 != 0); break;
+        default: by_mode((float2 *)nullptr, g.bf3 != 0); break;
+        }
+    }
+    MGB_CUDA_CHECK(cudaGetLastError());
+    return MGB_OK;
+}
+
+// Every pre-pass phase over the tables at device area `d`: clearing and the
+// statistics as one launch each, the scan and the slicing as one typed
+// launch per segment, the estimate and the choice before the slicing.
 static int pre_launch(const PreLayout &L, size_t npre, size_t nch, const uint8_t *d, cudaStream_t s) {
     const PreJob *dpre = (const PreJob *)(d + L.o_pre);
     for (int ph = 0; ph < PRE_PHASES; ++ph) {
@@ -2228,6 +2353,11 @@ static int pre_launch(const PreLayout &L, size_t npre, size_t nch, const uint8_t
             }
             k_oz_choose_multi<<<((int)nch + 127) / 128, 128, 0, s>>>((const ChooseJob *)(d + L.o_ch), (int)nch);
             MGB_CUDA_CHECK(cudaGetLastError());
+        }
+        if (ph == PRE_SCALE || ph == PRE_SLICE) {
+            for (const PreSegment &g : L.seg)
+                if (int st = seg_launch(g, ph, dpre, d, s)) return st;
+            continue;
         }
         if (L.blocks[ph] == 0) continue;
         if (L.blocks[ph] > INT32_MAX) return fail(MGB_ERR_UNSUPPORTED, "batch: pre-pass grid too large");
