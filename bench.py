@@ -1160,6 +1160,10 @@ def main():
     bf16_peak, hbm_peak, peak_kind = peaks()
     achieved = tensor_flops / (gemm_ms / 1e3) / 1e12
     traffic = ncu_traffic(S)
+    # pre-pass bytes: both operands read by the exponent scan and again by the
+    # slicer, S bf16 digit planes written (A: M x 2K, B embedded: 2N x 2K)
+    prepass_bytes = 2.0 * (A.numel() + B.numel()) * 16 + S * 2.0 * (n * 2 * 8192 + 2 * n * 2 * 8192)
+    prepass_ms = statistics.mean(pre)
 
     native = flops / (native_ms / 1e3) / 1e12
     fp64 = fp64_peaks(dev, target_ms=20.0)
@@ -1243,7 +1247,9 @@ def main():
                     "result_matches_device_run": e2e_ok, "phases": e2e_phases},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": achieved / bf16_peak, "traffic": traffic, "peak_kind": f"bf16 dense burst ({peak_kind})",
-                         "kernel": "k_oz_gemm", "kernel_ms": gemm_ms, "prepass_ms": statistics.mean(pre),
+                         "kernel": "k_oz_gemm", "kernel_ms": gemm_ms, "prepass_ms": prepass_ms,
+                         "prepass_bytes": prepass_bytes, "prepass_gbs": prepass_bytes / (prepass_ms / 1e3) / 1e9,
+                         "prepass_frac_of_hbm": prepass_bytes / (prepass_ms / 1e3) / 1e9 / hbm_peak,
                          "work": f"2 x {pairs} slice pairs x M x 2N x 2K bf16 flops per launch"},
             "serving": {"p50_ms": serving["served_emulated_best"]["p50_ms"],
                         "p99_ms": serving["served_emulated_best"]["p99_ms"],
