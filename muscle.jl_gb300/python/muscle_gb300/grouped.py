@@ -128,12 +128,13 @@ class Group:
         tables), then record execute() into a CUDA graph (with parts > 1 the
         parts become parallel branches of the graph).
 
-        On a 4096-member PEPS batch (148 plans) parts=4, persistent=False was
-        the fastest schedule on GB300 (ComplexF64 116 ms against 141 ms for
-        one persistent launch after all pre-passes): the HBM-bound pre-passes
-        of some buckets then overlap the tensor-core work of others. Without
-        arguments the group's `schedule` is used (set by
-        ``Autotuner.schedule``)."""
+        On a 4096-member PEPS batch, parts=4 or 8 with persistent=False was
+        the fastest schedule on GB300 (ComplexF64 97.8 ms against 109.6 ms
+        for one persistent launch per kernel variant after all pre-passes):
+        the HBM-bound pre-passes of some buckets then overlap the
+        tensor-core work of others, which a persistent launch, holding every
+        SM, leaves no room for. Without arguments the group's `schedule` is
+        used (set by ``Autotuner.schedule``)."""
         if parts is None:
             parts = self.schedule[0]
         if persistent is None:
