@@ -59,13 +59,13 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU work of the baseline sample")
     ap.add_argument("--workload", default="precision",
                     choices=["precision", "peps", "serve", "config2", "kernel", "permute", "hadamard", "unary", "fp64",
-                             "blocks", "shortk"],
+                             "blocks", "shortk", "simple_update"],
                     help="precision: the headline line; peps / serve: batching and serving forms; config2: "
                          "plain shapes that permute; kernel / permute: one contraction of the precision "
                          "workload at --n / the permutation of A(a,b,c,d,e) with e = --perm-e (profiling cases); "
                          "hadamard / unary: broadcast product / partial sums of a 4.3 GB array; blocks: the "
                          "precision workload at --n/2 contracted whole and block by block; shortk: 8192 x --k x 8192 "
-                         "(GEMM epilogue rate)")
+                         "(GEMM epilogue rate); simple_update: one MPS bond update (contractions, SVD, absorb)")
     ap.add_argument("--form", default="ozaki", help="form of --workload kernel")
     ap.add_argument("--band", type=int, default=0, help="rasterisation band of --workload kernel (0: default)")
     ap.add_argument("--perm-e", type=int, default=32, help="extent of label e in --workload permute")
@@ -650,6 +650,75 @@ def config2_bench(dev, steps=3):
     return res
 
 
+def simple_update_bench(dev, steps=20, warmup=3, chis=(16, 32, 64, 128)):
+    """Muscle's simple_update (src/Operations/simple_update.jl:35-82) on one
+    MPS bond: A(p1, l, b) and B(p2, b, r) ComplexF64 with bond chi, a random
+    two-site gate G(p1, p2, q1, q2), truncation to chi, normalisation and an
+    equal absorb. Device time per update (CUDA events around `steps` updates
+    issued from the host, plan creation included) against the CPU
+    restatement of the same update (numpy contractions, LAPACK SVD), and the
+    error of the reconstructed two-site tensor against it."""
+    import torch
+
+    import muscle_gb300 as m
+    from oracle import muscle_ref as ref
+
+    ia, ib, ig = ["p1", "l", "b"], ["p2", "b", "r"], ["p1", "p2", "q1", "q2"]
+    kw = dict(maxdim=None, normalize=True, absorb="equally")
+    res = {}
+    for chi in chis:
+        rng = np.random.default_rng(chi)
+
+        def r(shape):
+            return np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+
+        a, b, g = r((2, chi, chi)), r((2, chi, chi)), r((2, 2, 2, 2))
+        A, B, G = (m.Tensor(torch.from_numpy(x).to(dev), i) for x, i in ((a, ia), (b, ib), (g, ig)))
+        kw["maxdim"] = chi
+        for _ in range(warmup):
+            m.simple_update(A, "p1", B, "p2", "b", G, "q1", "q2", **kw)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            U, V = m.simple_update(A, "p1", B, "p2", "b", G, "q1", "q2", **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        reps, t0 = 0, time.perf_counter()
+        while reps < 3 or (time.perf_counter() - t0 < 1.0 and reps < steps):
+            (Uo, lu), (Vo, lv) = ref.simple_update(a, ia, "p1", b, ib, "p2", "b", g, ig, "q1", "q2", **kw)
+            reps += 1
+        cpu_ms = (time.perf_counter() - t0) / reps * 1e3
+        out = ["p1", "l", "p2", "r"]
+        got = ref.contract(U.data.cpu().numpy(), lu, V.data.cpu().numpy(), lv, out)
+        err = ref.rel_fro(got, ref.contract(Uo, lu, Vo, lv, out))
+        # the SVD step alone on the same 2chi x 2chi matrix: this library's
+        # Jacobi kernel, and torch.linalg.svd (cuSOLVER) for comparison
+        theta = m.Tensor(torch.from_numpy(r((2, chi, 2, chi))).to(dev), ["p1", "l", "p2", "r"])
+        reps_svd = 3
+
+        def timed(f):
+            f()
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(reps_svd):
+                f()
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps_svd
+
+        svd_ms = timed(lambda: m.tensor_svd_thin(theta, ["p1", "l"], ["p2", "r"]))
+        mat = theta.data.reshape(2 * chi, 2 * chi)
+        lib_ms = timed(lambda: torch.linalg.svd(mat, full_matrices=False))
+        res[f"chi{chi}"] = {"theta": [2 * chi, 2 * chi], "ms_per_update": ms, "cpu_ms_per_update": cpu_ms,
+                            "cpu_reps": reps, "speedup_vs_cpu": cpu_ms / ms, "rel_err_vs_cpu": err,
+                            "svd_ms": svd_ms, "torch_linalg_svd_ms": lib_ms, "status": m.device_status(dev)}
+    return {"cpu_baseline": {"kind": "port", "cores": os.cpu_count(),
+                             "sample": "the same update through numpy (OpenBLAS) and LAPACK's SVD"},
+            "updates": res}
+
+
 def blocks_bench(dev, n=4096, steps=3, warmup=1):
     """The precision workload at M = N = n (K = 8192) contracted whole and
     block by block (block_einsum: every block pair in one group, partial
@@ -947,6 +1016,9 @@ def main():
         elif args.workload == "hadamard":
             res = hadamard_case(dev, args.steps, args.warmup)
             metric = "hadamard (broadcast product) GB/s"
+        elif args.workload == "simple_update":
+            res = simple_update_bench(dev, max(args.steps, 10), args.warmup)
+            metric = "simple_update ms per MPS bond update (ComplexF64) against the CPU restatement"
         elif args.workload == "blocks":
             res = blocks_bench(dev, args.n // 2)
             metric = "block-partitioned contraction TFLOP/s against the whole contraction"

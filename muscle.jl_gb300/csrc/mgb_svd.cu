@@ -57,29 +57,47 @@ __device__ __forceinline__ double abs_of(double2 g) { return hypot(g.x, g.y); }
 __device__ __forceinline__ int circle(int i, int r, int nn) { return i == 0 ? 0 : (i - 1 + r) % (nn - 1) + 1; }
 
 // W: M x N (column-major, M >= N), V: N x N. info[0] = sweeps used.
+// A round has three phases: the warps compute the inner products of their
+// pairs; one thread per pair computes its rotation (the scalar square roots
+// and divisions run once per pair, not once per lane: on a GPU whose FP64
+// pipe retires under two operations per clock per SM they cost more than
+// the vector work of small matrices); the warps apply the rotations.
 template <typename T>
 __global__ void __launch_bounds__(kSvdThreads) k_svd_jacobi(T *__restrict__ W, int M, int N, T *__restrict__ V,
                                                             double tol, int32_t *info) {
+    constexpr int kPairs = kSvdMaxCols / 2;
     __shared__ int rotated;
+    __shared__ double pa[kPairs], pb[kPairs], pc[kPairs];
+    __shared__ T pg[kPairs], pse[kPairs], psec[kPairs];
+    __shared__ unsigned char pdo[kPairs];
     const int nn = N + (N & 1);
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
     for (int64_t i = threadIdx.x; i < (int64_t)N * N; i += blockDim.x)
         V[i] = (i % (N + 1) == 0) ? one_of(T()) : zero_of(T());
+    auto pair = [&](int pi, int r, int &p, int &q) {
+        p = circle(pi, r, nn);
+        q = circle(nn - 1 - pi, r, nn);
+        if (p > q) {
+            const int t = p;
+            p = q;
+            q = t;
+        }
+    };
     int sweep = 0;
     for (; sweep < kMaxSweeps; ++sweep) {
         __syncthreads();  // every thread has read the previous sweep's flag
         if (threadIdx.x == 0) rotated = 0;
         __syncthreads();
         for (int r = 0; r + 1 < nn; ++r) {
+            // inner products of the round's pairs
             for (int pi = warp; pi < nn / 2; pi += nw) {
-                int p = circle(pi, r, nn), q = circle(nn - 1 - pi, r, nn);
-                if (p >= N || q >= N) continue;  // the padding player of an odd N
-                if (p > q) {
-                    const int t = p;
-                    p = q;
-                    q = t;
+                int p, q;
+                pair(pi, r, p, q);
+                if (q >= N) {  // the padding player of an odd N
+                    if (lane == 0) pg[pi] = zero_of(T());
+                    continue;
                 }
-                T *wp = W + (int64_t)p * M, *wq = W + (int64_t)q * M;
+                const T *wp = W + (int64_t)p * M, *wq = W + (int64_t)q * M;
                 double a = 0.0, b = 0.0;
                 T g = zero_of(T());
                 for (int i = lane; i < M; i += 32) {
@@ -91,15 +109,43 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_jacobi(T *__restrict__ W, i
                 a = warp_sum(a);
                 b = warp_sum(b);
                 g = warp_sum(g);
+                if (lane == 0) {
+                    pa[pi] = a;
+                    pb[pi] = b;
+                    pg[pi] = g;
+                }
+            }
+            __syncthreads();
+            // rotations, one thread per pair
+            for (int pi = threadIdx.x; pi < nn / 2; pi += blockDim.x) {
+                const double a = pa[pi], b = pb[pi];
+                const T g = pg[pi];
                 const double gabs = abs_of(g);
-                if (!(gabs > tol * sqrt(a * b)) || gabs == 0.0) continue;  // orthogonal (uniform in the warp)
+                if (!(gabs > tol * sqrt(a * b)) || gabs == 0.0) {  // orthogonal (or the padding pair)
+                    pdo[pi] = 0;
+                    continue;
+                }
                 // [w_p, w_q] <- [w_p, w_q] J, J = [[c, s e], [-s conj(e), c]], e = g / |g|:
                 // makes w_p^H w_q vanish (c, s from the smaller root of t^2 + 2 zeta t - 1)
                 const double zeta = (b - a) / (2.0 * gabs);
                 const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
                 const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
                 const T e = phase_of(g, gabs);
-                const T se = sscale(e, s), sec = sscale(sconj(e), -s);
+                pc[pi] = c;
+                pse[pi] = sscale(e, s);
+                psec[pi] = sscale(sconj(e), -s);
+                pdo[pi] = 1;
+                rotated = 1;
+            }
+            __syncthreads();
+            // apply them to the columns of W and V
+            for (int pi = warp; pi < nn / 2; pi += nw) {
+                if (!pdo[pi]) continue;
+                int p, q;
+                pair(pi, r, p, q);
+                const double c = pc[pi];
+                const T se = pse[pi], sec = psec[pi];
+                T *wp = W + (int64_t)p * M, *wq = W + (int64_t)q * M;
                 for (int i = lane; i < M; i += 32) {
                     const T x = wp[i], y = wq[i];
                     wp[i] = sadd(sscale(x, c), smul(sec, y));
@@ -111,7 +157,6 @@ __global__ void __launch_bounds__(kSvdThreads) k_svd_jacobi(T *__restrict__ W, i
                     vp[i] = sadd(sscale(x, c), smul(sec, y));
                     vq[i] = sadd(smul(se, x), sscale(y, c));
                 }
-                if (lane == 0) rotated = 1;
             }
             __syncthreads();
         }
