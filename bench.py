@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--band", type=int, default=0, help="rasterisation band of --workload kernel (0: default)")
     ap.add_argument("--perm-e", type=int, default=32, help="extent of label e in --workload permute")
     ap.add_argument("--k", type=int, default=8, help="contracted extent of --workload shortk")
+    ap.add_argument("--chi", type=int, default=0, help="bond dimension of --workload simple_update (0: 16, 32, 64, 128)")
     ap.add_argument("--serve-seconds", type=float, default=1.5, help="per offered rate in the serving sweep")
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--serve-pool", type=int, default=4096, help="distinct requests of the serving workload")
@@ -1017,7 +1018,8 @@ def main():
             res = hadamard_case(dev, args.steps, args.warmup)
             metric = "hadamard (broadcast product) GB/s"
         elif args.workload == "simple_update":
-            res = simple_update_bench(dev, max(args.steps, 10), args.warmup)
+            res = simple_update_bench(dev, max(args.steps, 1), args.warmup,
+                                      (args.chi,) if args.chi > 0 else (16, 32, 64, 128))
             metric = "simple_update ms per MPS bond update (ComplexF64) against the CPU restatement"
         elif args.workload == "blocks":
             res = blocks_bench(dev, args.n // 2)
