@@ -7,51 +7,84 @@
 // reduction: y(o) = sum_r x(off_o + off_r). Memory-bound.
 #include <algorithm>
 
+#include "mgb_fxsum.h"
 #include "mgb_internal.h"
 
 namespace mgb {
 
+constexpr int UU = 4;  // loads in flight per thread
+
+// Accumulators. Float32 / ComplexF32 add in FP32 into UU independent partial
+// sums. Float64 / ComplexF64 add into fixed-point sums on the integer pipes
+// (mgb_fxsum.h): GB300's FP64 pipe would bound an FP64 sum at about half the
+// HBM rate, and the fixed-point sum is also exact within 10 binades of the
+// largest term and independent of the order. One such sum per thread and component.
 template <typename T>
 struct Acc;
-template <>
-struct Acc<float> {
-    using V = float;
-    __device__ static V zero() { return 0.f; }
-    __device__ static V add(V a, V b) { return a + b; }
+template <typename F>
+struct AccFp {
+    using V = F;
+    static constexpr int kParts = UU;
+    __device__ static V zero() { return F(0); }
+    __device__ static void push(V &a, F x) { a += x; }
+    __device__ static void merge(V &a, V b) { a += b; }
+    __device__ static V shfl(V a, int d) { return __shfl_down_sync(0xffffffffu, a, d); }
+    __device__ static F out(V a) { return a; }
 };
 template <>
-struct Acc<double> {
-    using V = double;
-    __device__ static V zero() { return 0.0; }
-    __device__ static V add(V a, V b) { return a + b; }
-};
+struct Acc<float> : AccFp<float> {};
 template <>
 struct Acc<float2> {
     using V = float2;
+    static constexpr int kParts = UU;
     __device__ static V zero() { return make_float2(0.f, 0.f); }
-    __device__ static V add(V a, V b) { return make_float2(a.x + b.x, a.y + b.y); }
+    __device__ static void push(V &a, float2 x) {
+        a.x += x.x;
+        a.y += x.y;
+    }
+    __device__ static void merge(V &a, V b) { push(a, b); }
+    __device__ static V shfl(V a, int d) {
+        return make_float2(__shfl_down_sync(0xffffffffu, a.x, d), __shfl_down_sync(0xffffffffu, a.y, d));
+    }
+    __device__ static float2 out(V a) { return a; }
+};
+__device__ __forceinline__ FxSum fx_shfl(const FxSum &a, int d) {
+    FxSum r;
+    r.lo = __shfl_down_sync(0xffffffffu, (unsigned long long)a.lo, d);
+    r.hi = __shfl_down_sync(0xffffffffu, (long long)a.hi, d);
+    r.e = __shfl_down_sync(0xffffffffu, a.e, d);
+    r.flags = __shfl_down_sync(0xffffffffu, a.flags, d);
+    return r;
+}
+template <>
+struct Acc<double> {
+    using V = FxSum;
+    static constexpr int kParts = 1;
+    __device__ static V zero() { return fx_zero(); }
+    __device__ static void push(V &a, double x) { fx_push(a, x); }
+    __device__ static void merge(V &a, const V &b) { fx_merge(a, b); }
+    __device__ static V shfl(const V &a, int d) { return fx_shfl(a, d); }
+    __device__ static double out(const V &a) { return fx_value(a); }
+};
+struct FxSum2 {
+    FxSum re, im;
 };
 template <>
 struct Acc<double2> {
-    using V = double2;
-    __device__ static V zero() { return make_double2(0.0, 0.0); }
-    __device__ static V add(V a, V b) { return make_double2(a.x + b.x, a.y + b.y); }
+    using V = FxSum2;
+    static constexpr int kParts = 1;
+    __device__ static V zero() { return FxSum2{fx_zero(), fx_zero()}; }
+    __device__ static void push(V &a, double2 x) {
+        fx_push(a.re, x.x);
+        fx_push(a.im, x.y);
+    }
+    __device__ static void merge(V &a, const V &b) {
+        fx_merge(a.re, b.re);
+        fx_merge(a.im, b.im);
+    }
+    __device__ static V shfl(const V &a, int d) { return FxSum2{fx_shfl(a.re, d), fx_shfl(a.im, d)}; }
+    __device__ static double2 out(const V &a) { return make_double2(fx_value(a.re), fx_value(a.im)); }
 };
-
-template <typename T>
-__device__ __forceinline__ T shfl_down(T v, int d);
-template <>
-__device__ __forceinline__ float shfl_down(float v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
-template <>
-__device__ __forceinline__ double shfl_down(double v, int d) { return __shfl_down_sync(0xffffffffu, v, d); }
-template <>
-__device__ __forceinline__ float2 shfl_down(float2 v, int d) {
-    return make_float2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
-}
-template <>
-__device__ __forceinline__ double2 shfl_down(double2 v, int d) {
-    return make_double2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
-}
 
 // Kernel arguments, in the parameter space (__grid_constant__): the mode
 // groups are indexed where they lie, never copied to local memory.
@@ -62,22 +95,21 @@ struct UnaryArgs {
     int64_t O, outer;    // outputs; rest.size()
 };
 
-constexpr int UU = 4;  // independent partial sums (loads in flight) per thread
-
 // One thread per output: consecutive threads take consecutive outputs, so
 // the loads are coalesced when Y's fastest mode is also X's (a sum over a
 // slower label); the fastest reduced mode is walked without division, four
-// elements at a time into independent partial sums.
+// loads in flight.
 template <typename T>
 __global__ void __launch_bounds__(256) k_unary_thread(const T *__restrict__ x, T *__restrict__ y,
                                                       const __grid_constant__ UnaryArgs a) {
+    using A = Acc<T>;
     const int64_t e0 = a.e0, s0 = a.s0;
     for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < a.O;
          o += (int64_t)gridDim.x * blockDim.x) {
         const T *xo = x + group_offset(a.go, 0, o);
-        T acc[UU];
+        typename A::V acc[A::kParts];
 #pragma unroll
-        for (int u = 0; u < UU; ++u) acc[u] = Acc<T>::zero();
+        for (int u = 0; u < A::kParts; ++u) acc[u] = A::zero();
         for (int64_t q = 0; q < a.outer; ++q) {
             const T *xq = xo + group_offset(a.rest, 0, q);
             int64_t r = 0;
@@ -86,28 +118,32 @@ __global__ void __launch_bounds__(256) k_unary_thread(const T *__restrict__ x, T
 #pragma unroll
                 for (int u = 0; u < UU; ++u) v[u] = __ldg(xq + (r + u) * s0);
 #pragma unroll
-                for (int u = 0; u < UU; ++u) acc[u] = Acc<T>::add(acc[u], v[u]);
+                for (int u = 0; u < UU; ++u) A::push(acc[u % A::kParts], v[u]);
             }
-            for (; r < e0; ++r) acc[0] = Acc<T>::add(acc[0], __ldg(xq + r * s0));
+            for (; r < e0; ++r) A::push(acc[0], __ldg(xq + r * s0));
         }
-        y[group_offset(a.go, 1, o)] = Acc<T>::add(Acc<T>::add(acc[0], acc[1]), Acc<T>::add(acc[2], acc[3]));
+#pragma unroll
+        for (int u = 1; u < A::kParts; ++u) A::merge(acc[0], acc[u]);
+        y[group_offset(a.go, 1, o)] = A::out(acc[0]);
     }
 }
 
 // One warp per output (long reductions): lanes take every 32nd element of
-// the fastest reduced mode, four at a time into independent partial sums.
+// the fastest reduced mode, four loads in flight; the lanes' sums are merged
+// by shuffles.
 template <typename T>
 __global__ void __launch_bounds__(256) k_unary_warp(const T *__restrict__ x, T *__restrict__ y,
                                                     const __grid_constant__ UnaryArgs a) {
+    using A = Acc<T>;
     const int lane = threadIdx.x % 32;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
     const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / 32;
     const int64_t e0 = a.e0, s0 = a.s0;
     for (int64_t o = warp; o < a.O; o += nwarps) {
         const T *xo = x + group_offset(a.go, 0, o);
-        T acc[UU];
+        typename A::V acc[A::kParts];
 #pragma unroll
-        for (int u = 0; u < UU; ++u) acc[u] = Acc<T>::zero();
+        for (int u = 0; u < A::kParts; ++u) acc[u] = A::zero();
         for (int64_t q = 0; q < a.outer; ++q) {
             const T *xq = xo + group_offset(a.rest, 0, q);
             int64_t r = lane;
@@ -116,14 +152,15 @@ __global__ void __launch_bounds__(256) k_unary_warp(const T *__restrict__ x, T *
 #pragma unroll
                 for (int u = 0; u < UU; ++u) v[u] = __ldg(xq + (r + 32 * u) * s0);
 #pragma unroll
-                for (int u = 0; u < UU; ++u) acc[u] = Acc<T>::add(acc[u], v[u]);
+                for (int u = 0; u < UU; ++u) A::push(acc[u % A::kParts], v[u]);
             }
-            for (; r < e0; r += 32) acc[0] = Acc<T>::add(acc[0], __ldg(xq + r * s0));
+            for (; r < e0; r += 32) A::push(acc[0], __ldg(xq + r * s0));
         }
-        T s = Acc<T>::add(Acc<T>::add(acc[0], acc[1]), Acc<T>::add(acc[2], acc[3]));
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) s = Acc<T>::add(s, shfl_down(s, d));
-        if (lane == 0) y[group_offset(a.go, 1, o)] = s;
+        for (int u = 1; u < A::kParts; ++u) A::merge(acc[0], acc[u]);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) A::merge(acc[0], A::shfl(acc[0], d));
+        if (lane == 0) y[group_offset(a.go, 1, o)] = A::out(acc[0]);
     }
 }
 
