@@ -105,7 +105,11 @@ int mgb_contract(mgb_plan plan, const void *A, const void *B, void *C,
 /* ---- unary contraction: Y[modes_y] = sum over the other modes of X --------
  * Repeated labels in X select a diagonal (test/integration/omeinsum.jl:6-100,
  * ext/MuscleOMEinsumExt.jl:25-38). modes_y must be distinct and a subset of
- * modes_x (ext/MuscleOMEinsumExt.jl:32). X and Y share the element type.   */
+ * modes_x (ext/MuscleOMEinsumExt.jl:32). X and Y share the element type.
+ * Float64 / ComplexF64 sums are fixed-point integers rounded once: exact
+ * while the terms lie within 10 binades of the largest one (otherwise within
+ * 2^-62 of the largest term per term), independent of the summation order,
+ * Inf / NaN as in an FP64 sum. Float32 / ComplexF32 add in FP32.           */
 int mgb_unary_plan(mgb_plan *plan, const mgb_tensor_desc *x,
                    const mgb_tensor_desc *y);
 int mgb_unary(mgb_plan plan, const void *X, void *Y, void *workspace,
