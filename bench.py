@@ -920,8 +920,9 @@ def hadamard_case(dev, steps, warmup):
 def unary_case(dev, steps, warmup):
     """unary_einsum partial sums of a ComplexF64 X(a,b,c) = 4096 x 1024 x 64
     (4.3 GB): over the middle label b (a thread per output, coalesced over a)
-    and over the contiguous label a (a warp per output). HBM-bound: algorithmic
-    bytes = read X + write Y."""
+    and over the contiguous label a (a warp per output). Fractions are of the
+    copy rate: algorithmic bytes = read X + write Y. The Float64 sums run as
+    fixed-point integers, bound by the integer ALU pipe short of HBM."""
     import torch
 
     import muscle_gb300 as m
