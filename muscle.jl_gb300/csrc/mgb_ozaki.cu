@@ -369,7 +369,7 @@ __device__ __forceinline__ void oz_scale_tile(const T *__restrict__ X, const OpG
     }
 }
 template <typename T>
-__global__ void __launch_bounds__(256, 3) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps, int32_t *emax,
+__global__ void __launch_bounds__(256, 4) k_oz_scale(const T *__restrict__ X, OpGeom g, int32_t *exps, int32_t *emax,
                                                   int2 *part) {
     __shared__ ScaleSmem sm;
     oz_scale_tile<T>(X, g, exps, emax, part, blockIdx.x, blockIdx.y, sm);
@@ -2044,7 +2044,7 @@ __device__ __forceinline__ int multi_job(const int64_t *__restrict__ start, int 
 // tile routine, shared memory and occupancy as the single-plan scan, for
 // many operands in one launch (no launch per operand, one tail for all).
 template <typename T>
-__global__ void __launch_bounds__(256, 3) k_oz_scale_multi(const PreJob *__restrict__ jobs,
+__global__ void __launch_bounds__(256, 4) k_oz_scale_multi(const PreJob *__restrict__ jobs,
                                                         const int64_t *__restrict__ start, int njobs) {
     __shared__ ScaleSmem sm;
     const int j = multi_job(start, njobs, blockIdx.x);
@@ -2058,7 +2058,7 @@ __global__ void __launch_bounds__(256, 3) k_oz_scale_multi(const PreJob *__restr
 // Slicing over a table of operand jobs of one element type, embedding and
 // form, as the single-plan slicer does it.
 template <typename T, int MODE, bool BF3>
-__global__ void __launch_bounds__(256, 3) k_oz_slice_multi(const PreJob *__restrict__ jobs,
+__global__ void __launch_bounds__(256, 4) k_oz_slice_multi(const PreJob *__restrict__ jobs,
                                                         const int64_t *__restrict__ start, int njobs) {
     __shared__ SliceSmemOf<T, MODE> sm;
     const int j = multi_job(start, njobs, blockIdx.x);
